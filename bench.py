@@ -1,0 +1,442 @@
+"""Benchmark of the GB300 Barnes–Hut step: steps/s at 16.7M bodies.
+
+Workload (default): 16,777,216 bodies, 70% Plummer (a=1) + 30% uniform in
+[-3,3]^3, equal masses, G=1, eps=0.005 (softening = eps^2), theta=0.5,
+dt=1e-3, dynamic bounds, no merges; seeded synthetic input (seed 3).
+
+One step = BarnesHut.step of the reference: compaction, AABB + Morton encode,
+radix sort, LBVH build, bottom-up fill, tree walk + update, merge, swap,
+launched as one CUDA graph.  The timed region holds exactly K steps between
+CUDA events recorded on the context stream, with a barrier and a device
+synchronise on both sides.  The inputs (16.7M bodies, 537 MB of bodies plus
+~5 GB of tree and sort buffers) are far larger than the 129 MB L2.
+
+Output: one JSON line (rank 0).  `--impl reference` times the reference
+algorithm on the host CPU cores (the C restatement under oracle/, since the
+reference itself is Java + OpenGL and cannot run here).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from gravity_gb300 import abi, ic  # noqa: E402
+
+METRIC = "steps/s at 16.7M bodies, learned-MAC vs plain theta walk at equal p99 accel error"
+WALK_FLOP_PER_INTERACTION = 20  # Nyland, Harris & Prins, GPU Gems 3 ch. 31
+
+
+def workload(name: str, n: int | None):
+    if name == "mixture":
+        n = n or 16777216
+        return dict(
+            name=f"plummer_uniform_mixture_n{n}",
+            bodies=lambda: ic.plummer_uniform(n, seed=3),
+            n=n,
+            params=abi.step_params(dt=1e-3, theta=0.5, softening=0.005 ** 2, bounds=abi.BOUNDS_DYNAMIC),
+        )
+    if name == "plummer":
+        n = n or 65536
+        return dict(
+            name=f"plummer_n{n}",
+            bodies=lambda: ic.plummer(n, seed=0),
+            n=n,
+            params=abi.step_params(dt=1e-3, theta=0.5, softening=0.01 ** 2, bounds=abi.BOUNDS_DYNAMIC),
+        )
+    if name == "uniform_merge":
+        n = n or 1048576
+        return dict(
+            name=f"uniform_merge_n{n}",
+            bodies=lambda: ic.uniform_merge(n, seed=1),
+            n=n,
+            params=abi.step_params(dt=5e-4, theta=0.7, softening=0.01 ** 2, mode=abi.MODE_MERGE,
+                                   bounds=abi.BOUNDS_STATIC),
+            bounds=np.array([-2, -2, -2, 2, 2, 2], np.float32),
+        )
+    raise ValueError(name)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": float(max(smax)) if smax else None,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("GBH_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, rank, world, local
+    return None, 0, 1, 0
+
+
+def barrier(dist, local):
+    if dist is not None:
+        import torch
+
+        if dist.get_backend() == "nccl":
+            dist.barrier(device_ids=[local])
+        else:
+            dist.barrier()
+        torch.cuda.synchronize() if torch.cuda.is_available() else None
+
+
+def max_over_ranks(dist, v: float, local) -> float:
+    if dist is None:
+        return v
+    import torch
+
+    dev = f"cuda:{local}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(wl, bodies, bounds, units, budget_s=20.0, threads=None):
+    """The reference algorithm (oracle port) on the host cores, on a bounded
+    sample: the full tree pipeline over all bodies plus the walk over every
+    `stride`-th body; steps/s extrapolates the walk to all bodies."""
+    from oracle import oracle as O
+
+    if threads:
+        O.set_threads(threads)
+    cores = O.get_threads()
+    o = O.OracleBarnesHut(wl["n"], bounds, units)
+    o.upload_bodies(bodies)
+    o.init()
+    p = wl["params"]
+    t0 = time.perf_counter()
+    o.stage_reset(p)
+    o.stage_prepare(p)
+    o.stage_sort()
+    o.stage_build()
+    o.stage_fill()
+    t_tree = time.perf_counter() - t0
+    n_live = o.read_sim_values().num_bodies
+    stride = 64
+    t0 = time.perf_counter()
+    inter = o.walk_sample(p, stride)
+    t_walk = time.perf_counter() - t0
+    sampled = (n_live + stride - 1) // stride
+    # grow the sample while it stays inside the budget
+    while t_tree + t_walk * 2 < budget_s and stride > 1:
+        stride //= 2
+        t0 = time.perf_counter()
+        inter = o.walk_sample(p, stride)
+        t_walk = time.perf_counter() - t0
+        sampled = (n_live + stride - 1) // stride
+    t_walk_full = t_walk * n_live / max(sampled, 1)
+    o.close()
+    return {
+        "value": 1.0 / (t_tree + t_walk_full),
+        "unit": "steps/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": f"tree pipeline over all {n_live} bodies ({t_tree:.2f} s) + walk over every {stride}-th body "
+                  f"({sampled} bodies, {t_walk:.2f} s, {inter} interactions), walk extrapolated to all bodies",
+        "t_tree_s": t_tree,
+        "t_walk_full_s": t_walk_full,
+    }
+
+
+def run_reference(args):
+    dist, rank, world, local = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    O.build()
+    wl = workload(args.workload, args.n)
+    bodies = wl["bodies"]()
+    bounds = wl.get("bounds", ic.exact_bounds(bodies))
+    units = abi.units(G=1.0)
+    o = O.OracleBarnesHut(wl["n"], bounds, units)
+    o.upload_bodies(bodies)
+    o.init()
+    p = wl["params"]
+    n_live = wl["n"]
+    stride = args.ref_stride
+
+    def one_step():
+        t0 = time.perf_counter()
+        o.stage_reset(p)
+        o.stage_prepare(p)
+        o.stage_sort()
+        o.stage_build()
+        o.stage_fill()
+        t1 = time.perf_counter()
+        o.walk_sample(p, stride)
+        t2 = time.perf_counter()
+        return (t1 - t0) + (t2 - t1) * stride
+
+    for _ in range(args.warmup):
+        one_step()
+    total = sum(one_step() for _ in range(args.steps))
+    ms = 1000.0 * total / args.steps
+    v = args.steps / total
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": v,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["name"], "n_bodies": wl["n"], "theta": p.theta, "mac": "plain"},
+        "cpu_baseline": {
+            "value": v,
+            "unit": "steps/s",
+            "cores": O.get_threads(),
+            "kind": "port",
+            "sample": f"each step: tree pipeline over all bodies + walk over every {stride}-th sorted body, "
+                      f"walk time scaled by {stride}",
+        },
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    dist, rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    from gravity_gb300 import BarnesHut
+
+    wl = workload(args.workload, args.n)
+    bodies = wl["bodies"]()
+    bounds = wl.get("bounds", ic.exact_bounds(bodies))
+    units = abi.units(G=1.0)
+    p = wl["params"]
+    bh = BarnesHut(wl["n"], bounds, units, device=local)
+    bh.upload_bodies(bodies)
+    bh.init()
+    stream = torch.cuda.ExternalStream(bh.stream, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        bh.step(p)
+    bh.synchronize()
+    st = bh.read_stats()
+    interactions = int(st.interactions)
+
+    clocks = ClockSampler(local)
+    barrier(dist, local)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    bh.step(p, count=args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(dist, local)
+    clk = clocks.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    ms_total = max_over_ranks(dist, ms_total, local)
+    ms_step = ms_total / args.steps
+    value = world * args.steps / (ms_total / 1000.0)
+    bh.synchronize()
+    st = bh.read_stats()
+
+    # per-stage times (CUDA events between eager stage launches on the context stream)
+    prof = [bh.step_profiled(p) for _ in range(3)]
+    stage_ms = {k: float(np.median([d[k] for d in prof])) for k in abi.STAGE_NAMES}
+    st_prof = bh.read_stats()
+    walk_ms = stage_ms["walk"]
+    walk_flop = WALK_FLOP_PER_INTERACTION * int(st_prof.interactions)
+    fp32_peak = None
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        peaks = {}
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    # FP32 FMA pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = walk_flop / (walk_ms / 1000.0) / 1e12
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    n_live = int(st_prof.alive)
+    sort_bytes = (8 + 24 * 8) * n_live
+    sort_gbs = sort_bytes / (stage_ms["sort"] / 1000.0) / 1e9
+
+    # e2e through the public API with host buffers: per step the parameters go
+    # host->device and the live positions + SimulationValues come back
+    pos_host = np.empty(wl["n"], dtype=abi.BODY_DTYPE)
+    e2e_steps = max(3, min(args.steps, 10))
+    barrier(dist, local)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bh.step(p)
+        pos_host[:] = bh.read_bodies()
+        bh.read_sim_values()
+    t1 = time.perf_counter()
+    e2e_val = max_over_ranks(dist, (t1 - t0), local)
+    e2e = {
+        "value": world * e2e_steps / e2e_val,
+        "unit": "steps/s",
+        "h2d_bytes_per_step": C.sizeof(abi.StepParams),
+        "d2h_bytes_per_step": wl["n"] * abi.BODY_DTYPE.itemsize + C.sizeof(abi.SimValues),
+    }
+    launches_per_step = 1 + 3 + 1 + 8 + 1 + 1 + 1 + 4  # reset, prepare x3, sort scan + 8 passes, build, fill, walk, merge x4
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, bodies, bounds, units, budget_s=args.cpu_budget)
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded ICs, numpy PCG64)",
+        "config": {
+            "workload": wl["name"],
+            "n_bodies": wl["n"],
+            "theta": p.theta,
+            "softening": p.softening,
+            "mac": "plain",
+            "l2": "inputs larger than L2 (bodies 537 MB, tree + sort buffers ~5 GB)",
+            "parallelism": f"replicas x{world}",
+        },
+        "gpu_launches": launches_per_step * args.steps,
+        "interactions_per_step": interactions,
+        "interactions_per_s": interactions * value / world,
+        "stage_ms": stage_ms,
+        "roofline": {
+            "kernel": "k_walk_plain",
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": fp32_peak,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak,
+            "traffic": None,
+            "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json",
+            "flop_per_interaction": WALK_FLOP_PER_INTERACTION,
+        },
+        "roofline_sort": {
+            "kernel": "k_sort_pass x8 + k_sort_scan",
+            "bound": "hbm",
+            "achieved": sort_gbs,
+            "peak": hbm_peak,
+            "unit": "GB/s",
+            "frac": sort_gbs / hbm_peak,
+            "traffic": None,
+            "bytes_per_pair": 8 + 24 * 8,
+        },
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+        "stats": abi.stats_to_dict(st),
+        "footprint_bytes": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mixture", choices=["mixture", "plummer", "uniform_merge"])
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-stride", type=int, default=256)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

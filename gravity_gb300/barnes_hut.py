@@ -1,0 +1,206 @@
+"""Host-side mirror of the reference's BarnesHut step interface over libgbh.so.
+
+The reference drives its GLSL pipeline from Java
+(src/main/java/com/grumbo/simulation/BarnesHut.java:99-173, GPU.java:172-1196).
+`BarnesHut` keeps that interface: construct with the body capacity, bounds and
+unit set (GPU.initGPU), upload bodies (GPU.uploadPlanetsData), `init()` and
+`step()`.  The per-stage methods carry the reference's stage names and run the
+stage entry points of the C ABI; the compaction, bounds update and Morton
+encode are one fused stage here (`partition_dead_bodies`).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import GbhError, check, lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class BarnesHut:
+    """One simulation context on one GPU (owns all its device memory)."""
+
+    def __init__(self, initial_num_bodies: int, bounds, units: abi.Units | None = None, device: int = 0):
+        self.n = int(initial_num_bodies)
+        b = np.ascontiguousarray(np.asarray(bounds, dtype=np.float32).reshape(-1))
+        if b.size != 6:
+            raise ValueError("bounds must hold 6 floats (min xyz, max xyz)")
+        self._bounds = (C.c_float * 6)(*b.tolist())
+        self.units = units if units is not None else abi.units()
+        h = C.c_void_p()
+        rc = lib().gbh_create(C.byref(h), self.n, self._bounds, C.byref(self.units), device)
+        if rc != 0:
+            raise GbhError(rc, (lib().gbh_last_error(None) or b"").decode())
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, rc):
+        check(rc, self._h)
+
+    # ---- lifecycle (GPU.initGPU / BarnesHut.init / BarnesHut.step) ----------
+    def upload_bodies(self, bodies: np.ndarray, offset: int = 0, chunk: int = 1 << 22):
+        b = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+        for s in range(0, len(b), chunk):
+            part = b[s : s + chunk]
+            self._chk(lib().gbh_upload_bodies(self._h, _ptr(part), len(part), offset + s))
+
+    def init(self):
+        self._chk(lib().gbh_init(self._h))
+
+    def step(self, params: abi.StepParams, count: int = 1):
+        self._chk(lib().gbh_step_n(self._h, C.byref(params), count))
+
+    def synchronize(self):
+        self._chk(lib().gbh_synchronize(self._h))
+
+    def clear_error(self):
+        self._chk(lib().gbh_clear_error(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().gbh_stream(self._h) or 0
+
+    # ---- stages, named after BarnesHut.java's private methods ----------------
+    def reset_values(self, p):
+        self._chk(lib().gbh_stage_reset(self._h, C.byref(p)))
+
+    def partition_dead_bodies(self, p):
+        """partitionDeadBodies + decrementDeadBodies + updateBounds + generateMortonCodes."""
+        self._chk(lib().gbh_stage_prepare(self._h, C.byref(p)))
+
+    def radix_sort(self):
+        self._chk(lib().gbh_stage_sort(self._h))
+
+    def build_binary_radix_tree(self):
+        self._chk(lib().gbh_stage_build(self._h))
+
+    def compute_com_and_location(self):
+        self._chk(lib().gbh_stage_fill(self._h))
+
+    def compute_force(self, p):
+        self._chk(lib().gbh_stage_walk(self._h, C.byref(p)))
+
+    def merge_bodies(self, p):
+        self._chk(lib().gbh_stage_merge(self._h, C.byref(p)))
+
+    def swap_body_buffers(self):
+        self._chk(lib().gbh_stage_swap(self._h))
+
+    # oracle-compatible aliases (the CPU oracle uses the same names)
+    stage_reset = reset_values
+    stage_prepare = partition_dead_bodies
+    stage_sort = radix_sort
+    stage_build = build_binary_radix_tree
+    stage_fill = compute_com_and_location
+    stage_walk = compute_force
+    stage_merge = merge_bodies
+    stage_swap = swap_body_buffers
+
+    def step_profiled(self, p) -> dict:
+        ms = (C.c_float * abi.NUM_STAGES)()
+        self._chk(lib().gbh_step_profiled(self._h, C.byref(p), ms))
+        return dict(zip(abi.STAGE_NAMES, [float(x) for x in ms]))
+
+    # ---- read-back -----------------------------------------------------------
+    def read_bodies(self, which=abi.BODIES_IN, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros(count, dtype=abi.BODY_DTYPE)
+        self._chk(lib().gbh_read_bodies(self._h, which, _ptr(out), count, offset))
+        return out
+
+    def read_leaf_nodes(self, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros(count, dtype=abi.NODE_DTYPE)
+        self._chk(lib().gbh_read_leaf_nodes(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_internal_nodes(self, count=None, offset=0) -> np.ndarray:
+        cap = max(self.n - 1, 1)
+        count = cap - offset if count is None else count
+        out = np.zeros(count, dtype=abi.NODE_DTYPE)
+        self._chk(lib().gbh_read_internal_nodes(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_sim_values(self) -> abi.SimValues:
+        s = abi.SimValues()
+        self._chk(lib().gbh_read_sim_values(self._h, C.byref(s)))
+        return s
+
+    def read_index(self, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros(count, dtype=np.uint32)
+        self._chk(lib().gbh_read_index(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_morton(self, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros(count, dtype=np.uint64)
+        self._chk(lib().gbh_read_morton(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_merge_tasks(self) -> np.ndarray:
+        cnt = C.c_uint32(0)
+        self._chk(lib().gbh_read_merge_tasks(self._h, None, 0, C.byref(cnt)))
+        out = np.zeros((cnt.value, 2), dtype=np.uint32)
+        if cnt.value:
+            self._chk(lib().gbh_read_merge_tasks(self._h, _ptr(out), cnt.value, C.byref(cnt)))
+        return out
+
+    def read_accel(self, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros((count, 4), dtype=np.float32)
+        self._chk(lib().gbh_read_accel(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_stats(self) -> abi.Stats:
+        s = abi.Stats()
+        self._chk(lib().gbh_read_stats(self._h, C.byref(s)))
+        return s
+
+    def device_ptrs(self) -> abi.DeviceBuffers:
+        d = abi.DeviceBuffers()
+        self._chk(lib().gbh_device_ptrs(self._h, C.byref(d)))
+        return d
+
+    def write_sim_values(self, s: abi.SimValues):
+        self._chk(lib().gbh_write_sim_values(self._h, C.byref(s)))
+
+    def write_index(self, idx: np.ndarray, offset=0):
+        a = np.ascontiguousarray(idx, dtype=np.uint32)
+        self._chk(lib().gbh_write_index(self._h, _ptr(a), len(a), offset))
+
+    def write_morton(self, keys: np.ndarray, offset=0):
+        a = np.ascontiguousarray(keys, dtype=np.uint64)
+        self._chk(lib().gbh_write_morton(self._h, _ptr(a), len(a), offset))
+
+    # ---- accuracy judge --------------------------------------------------------
+    def direct_sum(self, params: abi.StepParams, sample: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(sample, dtype=np.uint32)
+        out = np.zeros((len(s), 3), dtype=np.float64)
+        self._chk(lib().gbh_direct_sum(self._h, C.byref(params), _ptr(s), len(s), _ptr(out)))
+        return out

@@ -1,0 +1,175 @@
+// gbh_common.cuh — device-side types and helpers shared by the step kernels.
+//
+// Arithmetic convention: the library is compiled with --fmad=false, so every
+// FP32 expression below rounds once per operation in source order, matching
+// the reference GLSL evaluated as IEEE FP32 (SH/compute/*, SH/common/common.glsl).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbh.h"
+
+#define GBH_NONE 0xFFFFFFFFu
+#define GBH_WARP 32
+#define GBH_WALK_STACK 192     // per-warp walk stack entries (tree height + 1 needed)
+#define GBH_MAX_TREE_HEIGHT_REF 64  // the reference fills 64 levels (GPU.java:41)
+
+// onesweep radix sort geometry (8-bit digits, 8 passes over the 63-bit key)
+#define SORT_BITS 8
+#define SORT_RADIX 256
+#define SORT_PASSES 8
+#define SORT_THREADS 256
+#define SORT_ITEMS 12
+#define SORT_TILE (SORT_THREADS * SORT_ITEMS)
+
+// fused compaction / bounds / encode geometry
+#define PREP_THREADS 256
+#define PREP_ITEMS 8
+#define PREP_TILE (PREP_THREADS * PREP_ITEMS)
+
+// Compact node record read by the walk: 32 bytes = one DRAM sector.
+struct __align__(16) WalkNode {
+    float4 cm;        // centre of mass xyz, mass
+    float half_side;  // getLongestSide(node), bh_force.comp:14-20
+    uint32_t child_a;
+    uint32_t child_b;
+    uint32_t count;   // bodies contained
+};
+
+// Device-resident state of one step (never read by the reference-facing
+// buffers; these are the library's own counters and scratch scalars).
+struct DevState {
+    uint32_t n_old;        // live count entering the step
+    uint32_t n_new;        // live count after compaction
+    uint32_t just_died;
+    uint32_t error_word;   // GBH_DEVERR_* (sticky)
+    uint32_t merge_conflicts;
+    uint32_t merged;
+    uint32_t oob;
+    uint32_t tree_height;
+    uint32_t max_stack;
+    uint32_t merge_tasks;
+    uint32_t sort_tiles[SORT_PASSES];  // onesweep tile tickets
+    uint32_t pad[2];
+    unsigned long long interactions;
+    unsigned long long opened;
+    unsigned long long mac_evals;
+};
+
+// Merge queue with the reference layout (MergeTasks: head, tail, uvec2[]),
+// common.glsl:117.
+struct MergeQueue {
+    uint32_t head;
+    uint32_t tail;
+    uint2 pairs[1];  // flexible
+};
+
+// Pointers handed to every kernel (by value).
+struct StepBuffers {
+    gbh_body* bodies_in;
+    gbh_body* bodies_out;
+    uint64_t* keys_in;    // MortonIn at step start
+    uint32_t* idx_in;     // IndexIn at step start
+    uint64_t* keys_out;   // the other buffer
+    uint32_t* idx_out;
+    gbh_node* leaf;
+    gbh_node* internal;
+    WalkNode* wnode;
+    float4* leaf_pm;      // sorted-order copy of posMass (leaf comMass)
+    float* leaf_rad;      // sorted-order radius(body)
+    gbh_sim_values* sim;
+    DevState* st;
+    const gbh_step_params* params;
+    MergeQueue* mq;
+    unsigned long long* mkeys;  // merge ordering keys (slot << 32 | seq)
+    uint32_t* locks;
+    uint32_t* conflicts;
+    float4* accel;
+    // compaction scratch
+    uint32_t* tile_dead;
+    float* tile_aabb;
+    // sort scratch
+    uint32_t* hist;         // [SORT_PASSES][SORT_RADIX]
+    uint32_t* bucket_base;  // [SORT_PASSES][SORT_RADIX]
+    uint32_t* lookback;     // [SORT_PASSES][sort_tiles_cap][SORT_RADIX]
+    uint32_t N;
+    uint32_t sort_tiles_cap;
+    uint32_t prep_tiles_cap;
+};
+
+// ---- GLSL built-in semantics (GLSL 4.30 §8.3) -------------------------------
+__device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+
+__device__ __forceinline__ void set_error(DevState* st, uint32_t bit) { atomicOr(&st->error_word, bit); }
+
+// expandBits21 / morton3D64, bh_morton.comp:6-21
+__device__ __forceinline__ uint64_t expand_bits21(uint32_t v) {
+    uint64_t x = (uint64_t)v & 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+    return !(isnan(x) || isnan(y) || isnan(z) || isinf(x) || isinf(y) || isinf(z));
+}
+
+// mortonEncodeKernel body, bh_morton.comp:238-262
+__device__ __forceinline__ uint64_t morton_encode(float px, float py, float pz, const float* mn, const float* mx) {
+    float p[3] = {px, py, pz};
+    uint32_t q[3];
+    const bool empty = mn[0] > mx[0];
+    const bool centre = !finite3(px, py, pz) || empty;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float pos = centre ? 0.5f * (mn[k] + mx[k]) : gclamp(p[k], mn[k], mx[k]);
+        float ext = gmax(mx[k] - mn[k], 1e-9f);
+        float nrm = (pos - mn[k]) / ext;
+        float f = gclamp(floorf(nrm * 2097151.0f), 0.0f, 2097151.0f);
+        q[k] = (uint32_t)floorf(f);
+    }
+    return (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
+}
+
+// radius(Body), common.glsl:228-230
+__device__ __forceinline__ float body_radius(float body_len_const, float m, float rho) {
+    return body_len_const * powf(m / rho, 1.0f / 3.0f);
+}
+
+// Body access as two 16-byte vectors (bodies are 32 bytes, 16-byte aligned).
+__device__ __forceinline__ float4 ld_pos_mass(const gbh_body* b, uint32_t i) {
+    return reinterpret_cast<const float4*>(b)[2 * (size_t)i];
+}
+__device__ __forceinline__ float4 ld_vel_density(const gbh_body* b, uint32_t i) {
+    return reinterpret_cast<const float4*>(b)[2 * (size_t)i + 1];
+}
+__device__ __forceinline__ void st_body(gbh_body* b, uint32_t i, float4 pm, float4 vd) {
+    float4* p = reinterpret_cast<float4*>(b) + 2 * (size_t)i;
+    p[0] = pm;
+    p[1] = vd;
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---- launchers (host), one translation unit each -----------------------------
+void launch_reset(const StepBuffers& b, cudaStream_t s);
+void launch_prepare(const StepBuffers& b, cudaStream_t s);
+void launch_sort(const StepBuffers& b, cudaStream_t s);
+void launch_build(const StepBuffers& b, cudaStream_t s);
+void launch_fill(const StepBuffers& b, cudaStream_t s);
+void launch_walk_plain(const StepBuffers& b, cudaStream_t s);
+void launch_merge(const StepBuffers& b, cudaStream_t s);
+void launch_init_index(uint32_t* idx, uint32_t N, gbh_sim_values* sim, const gbh_units* units_dev, cudaStream_t s);
+void launch_direct_sum(const gbh_body* bodies, uint32_t n_bodies, const uint32_t* sample, uint32_t count,
+                       float G, float soft, double* partial, double* out, uint32_t chunks, cudaStream_t s);

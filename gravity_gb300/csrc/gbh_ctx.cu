@@ -1,0 +1,583 @@
+// gbh_ctx.cu — host side of the C ABI (include/gbh.h): context, device arena,
+// stage sequencing, CUDA-graph capture of the whole step, read-back.
+//
+// Replaces the reference's host orchestration: BarnesHut.step/init
+// (src/main/java/com/grumbo/simulation/BarnesHut.java:99-173), the GPU object
+// registry and buffer swaps (src/main/java/com/grumbo/gpu/GPU.java:172-358,
+// 1060-1196).  Where the reference issues ~140 dispatches with a full memory
+// barrier after each, one step here is one CUDA-graph launch of ~20 kernels.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "gbh_common.cuh"
+#include "gbh_ctx.h"
+
+static thread_local std::string g_create_error;
+
+// ---------------------------------------------------------------------------
+// error helpers
+
+static int fail(gbh_ctx* c, int code, const std::string& msg) {
+    if (c)
+        c->last_error = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                          \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return fail((ctx), GBH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// arena
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct ArenaPlan {
+    size_t total = 0;
+    size_t add(size_t bytes) {
+        size_t off = total;
+        total = align_up(total + bytes, 256);
+        return off;
+    }
+};
+
+StepBuffers ctx_buffers(const gbh_ctx* c) {
+    StepBuffers b;
+    b.bodies_in = c->bodies[c->bin];
+    b.bodies_out = c->bodies[1 - c->bin];
+    b.keys_in = c->keys[c->iin];
+    b.idx_in = c->idx[c->iin];
+    b.keys_out = c->keys[1 - c->iin];
+    b.idx_out = c->idx[1 - c->iin];
+    b.leaf = c->leaf;
+    b.internal = c->internal;
+    b.wnode = c->wnode;
+    b.leaf_pm = c->leaf_pm;
+    b.leaf_rad = c->leaf_rad;
+    b.sim = c->sim;
+    b.st = c->st;
+    b.params = c->params_dev;
+    b.mq = c->mq;
+    b.mkeys = c->mkeys;
+    b.locks = c->locks;
+    b.conflicts = c->conflicts;
+    b.accel = c->accel;
+    b.tile_dead = c->tile_dead;
+    b.tile_aabb = c->tile_aabb;
+    b.hist = c->hist;
+    b.bucket_base = c->bucket_base;
+    b.lookback = c->lookback;
+    b.N = c->N;
+    b.sort_tiles_cap = c->sort_tiles_cap;
+    b.prep_tiles_cap = c->prep_tiles_cap;
+    return b;
+}
+
+static int check_launch(gbh_ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, GBH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return GBH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage enqueue (shared by eager stage calls, profiling and graph capture)
+
+int enqueue_reset(gbh_ctx* c) {
+    launch_reset(ctx_buffers(c), c->stream);
+    return check_launch(c, "reset");
+}
+
+int enqueue_prepare(gbh_ctx* c) {
+    launch_prepare(ctx_buffers(c), c->stream);
+    c->iin = 1 - c->iin;  // GPU.swapMortonAndIndexBuffers after the partition
+    return check_launch(c, "prepare");
+}
+
+int enqueue_sort(gbh_ctx* c) {
+    CUDA_TRY(c, cudaMemsetAsync(c->lookback, 0, c->lookback_bytes, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->st->sort_tiles, 0, sizeof(c->st->sort_tiles), c->stream));
+    launch_sort(ctx_buffers(c), c->stream);
+    return check_launch(c, "sort");
+}
+
+int enqueue_build(gbh_ctx* c) {
+    launch_build(ctx_buffers(c), c->stream);
+    return check_launch(c, "build");
+}
+
+int enqueue_fill(gbh_ctx* c) {
+    launch_fill(ctx_buffers(c), c->stream);
+    return check_launch(c, "fill");
+}
+
+int enqueue_walk(gbh_ctx* c) {
+    if (c->mac_mode == GBH_MAC_PLAIN) {
+        launch_walk_plain(ctx_buffers(c), c->stream);
+    } else {
+        int rc = enqueue_walk_learned(c);
+        if (rc) return rc;
+    }
+    return check_launch(c, "walk");
+}
+
+int enqueue_merge(gbh_ctx* c) {
+    launch_merge(ctx_buffers(c), c->stream);
+    return check_launch(c, "merge");
+}
+
+int enqueue_swap(gbh_ctx* c) {
+    c->bin = 1 - c->bin;  // GPU.swapBodyBuffers
+    return GBH_OK;
+}
+
+typedef int (*stage_fn)(gbh_ctx*);
+static const stage_fn k_stages[GBH_NUM_STAGES] = {enqueue_reset, enqueue_prepare, enqueue_sort, enqueue_build,
+                                                  enqueue_fill,  enqueue_walk,    enqueue_merge, enqueue_swap};
+
+static int enqueue_step(gbh_ctx* c) {
+    for (int s = 0; s < GBH_NUM_STAGES; ++s) {
+        int rc = k_stages[s](c);
+        if (rc) return rc;
+    }
+    return GBH_OK;
+}
+
+static int upload_params(gbh_ctx* c, const gbh_step_params* p) {
+    if (!p) return fail(c, GBH_ERR_INVALID, "null step params");
+    if (p->merging_collision_or_neither > 2 || p->static_or_dynamic > 1 || p->mac_mode > 2 || p->precision_mode > 1)
+        return fail(c, GBH_ERR_INVALID, "step params: enum out of range");
+    if ((p->flags & GBH_FLAG_STORE_ACCEL) && !c->accel) return fail(c, GBH_ERR_INVALID, "accel buffer missing");
+    if (p->mac_mode != GBH_MAC_PLAIN && !c->mac_ready && p->mac_mode == GBH_MAC_LEARNED)
+        return fail(c, GBH_ERR_STATE, "learned MAC selected but no weights were set");
+    // pageable source: the copy is staged before cudaMemcpyAsync returns
+    if (!c->params_valid || memcmp(&c->params_host, p, sizeof(*p)) != 0) {
+        CUDA_TRY(c, cudaMemcpyAsync(c->params_dev, p, sizeof(*p), cudaMemcpyHostToDevice, c->stream));
+        c->params_host = *p;
+        c->params_valid = true;
+    }
+    c->mac_mode = p->mac_mode;
+    return GBH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int gbh_abi_version(void) { return GBH_ABI_VERSION; }
+
+const char* gbh_last_error(gbh_ctx* c) { return c ? c->last_error.c_str() : g_create_error.c_str(); }
+
+int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units* units, int device) {
+    if (!out) return fail(nullptr, GBH_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (!bounds || !units) return fail(nullptr, GBH_ERR_INVALID, "bounds/units is null");
+    if (n == 0 || n > (1u << 30)) return fail(nullptr, GBH_ERR_INVALID, "initial_num_bodies must be in [1, 2^30]");
+    if (units->density == 0.0f || units->len == 0.0f)
+        return fail(nullptr, GBH_ERR_INVALID, "units: density and len must be non-zero");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(nullptr, GBH_ERR_CUDA, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(nullptr, GBH_ERR_INVALID, "device index out of range");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fail(nullptr, GBH_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+
+    gbh_ctx* c = new gbh_ctx();
+    c->device = device;
+    c->N = n;
+    c->prep_tiles_cap = (n + PREP_TILE - 1) / PREP_TILE;
+    c->sort_tiles_cap = (n + SORT_TILE - 1) / SORT_TILE;
+    const uint32_t ni = n > 1 ? n - 1 : 1;
+
+    ArenaPlan A;
+    size_t o_bodies0 = A.add((size_t)n * 32), o_bodies1 = A.add((size_t)n * 32);
+    size_t o_keys0 = A.add((size_t)n * 8), o_keys1 = A.add((size_t)n * 8);
+    size_t o_idx0 = A.add((size_t)n * 4), o_idx1 = A.add((size_t)n * 4);
+    size_t o_leaf = A.add((size_t)n * 80), o_int = A.add((size_t)ni * 80);
+    size_t o_wnode = A.add((size_t)ni * sizeof(WalkNode));
+    size_t o_lpm = A.add((size_t)n * 16), o_lrad = A.add((size_t)n * 4);
+    size_t o_sim = A.add(sizeof(gbh_sim_values)), o_st = A.add(sizeof(DevState));
+    size_t o_par = A.add(sizeof(gbh_step_params));
+    size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8);
+    size_t o_locks = A.add((size_t)n * 4), o_conf = A.add((size_t)n * 4);
+    size_t o_accel = A.add((size_t)n * 16);
+    size_t o_tdead = A.add((size_t)c->prep_tiles_cap * 4), o_taabb = A.add((size_t)c->prep_tiles_cap * 24);
+    size_t o_hist = A.add(SORT_PASSES * SORT_RADIX * 4), o_bbase = A.add(SORT_PASSES * SORT_RADIX * 4);
+    c->lookback_bytes = (size_t)SORT_PASSES * c->sort_tiles_cap * SORT_RADIX * 4;
+    size_t o_lb = A.add(c->lookback_bytes);
+    e = cudaMalloc(&c->arena, A.total);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(nullptr, GBH_ERR_OOM, "cudaMalloc of " + std::to_string(A.total) + " bytes failed");
+    }
+    c->arena_bytes = A.total;
+    char* base = (char*)c->arena;
+    c->bodies[0] = (gbh_body*)(base + o_bodies0);
+    c->bodies[1] = (gbh_body*)(base + o_bodies1);
+    c->keys[0] = (uint64_t*)(base + o_keys0);
+    c->keys[1] = (uint64_t*)(base + o_keys1);
+    c->idx[0] = (uint32_t*)(base + o_idx0);
+    c->idx[1] = (uint32_t*)(base + o_idx1);
+    c->leaf = (gbh_node*)(base + o_leaf);
+    c->internal = (gbh_node*)(base + o_int);
+    c->wnode = (WalkNode*)(base + o_wnode);
+    c->leaf_pm = (float4*)(base + o_lpm);
+    c->leaf_rad = (float*)(base + o_lrad);
+    c->sim = (gbh_sim_values*)(base + o_sim);
+    c->st = (DevState*)(base + o_st);
+    c->params_dev = (gbh_step_params*)(base + o_par);
+    c->mq = (MergeQueue*)(base + o_mq);
+    c->mkeys = (unsigned long long*)(base + o_mkeys);
+    c->locks = (uint32_t*)(base + o_locks);
+    c->conflicts = (uint32_t*)(base + o_conf);
+    c->accel = (float4*)(base + o_accel);
+    c->tile_dead = (uint32_t*)(base + o_tdead);
+    c->tile_aabb = (float*)(base + o_taabb);
+    c->hist = (uint32_t*)(base + o_hist);
+    c->bucket_base = (uint32_t*)(base + o_bbase);
+    c->lookback = (uint32_t*)(base + o_lb);
+
+    sort_setup();
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->arena, 0, A.total, c->stream);
+    // SimulationValues as packed by GPU.packValues (GPU.java:1096-1143)
+    gbh_sim_values sv;
+    memset(&sv, 0, sizeof(sv));
+    sv.num_bodies = n;
+    sv.initial_num_bodies = n;
+    for (int k = 0; k < 3; ++k) {
+        sv.bounds_min[k] = bounds[k];
+        sv.bounds_max[k] = bounds[3 + k];
+    }
+    sv.unit_mass = units->mass;
+    sv.unit_density = units->density;
+    sv.unit_len = units->len;
+    sv.unit_time = units->time;
+    sv.camera_scale = units->camera_scale;
+    c->units = *units;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->sim, &sv, sizeof(sv), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        std::string m = std::string("create: ") + cudaGetErrorString(e);
+        gbh_destroy(c);
+        return fail(nullptr, GBH_ERR_CUDA, m);
+    }
+    *out = c;
+    return GBH_OK;
+}
+
+int gbh_destroy(gbh_ctx* c) {
+    if (!c) return GBH_ERR_INVALID;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    mac_release(c);
+    if (c->arena) cudaFree(c->arena);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return GBH_OK;
+}
+
+int gbh_upload_bodies(gbh_ctx* c, const gbh_body* host, uint32_t count, uint32_t offset) {
+    if (!c || !host) return fail(c, GBH_ERR_INVALID, "null argument");
+    if ((uint64_t)offset + count > c->N) return fail(c, GBH_ERR_INVALID, "upload range exceeds initial_num_bodies");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(c->bodies[c->bin] + offset, host, (size_t)count * sizeof(gbh_body),
+                                cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_init(gbh_ctx* c) {
+    if (!c) return fail(c, GBH_ERR_INVALID, "null context");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_init_index(c->idx[c->iin], c->N, c->sim, &c->units, c->stream);
+    int rc = check_launch(c, "init");
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->inited = true;
+    return GBH_OK;
+}
+
+static int graph_key(const gbh_ctx* c) { return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2); }
+
+int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1); }
+
+int gbh_step_n(gbh_ctx* c, const gbh_step_params* p, uint32_t count) {
+    if (!c) return fail(c, GBH_ERR_INVALID, "null context");
+    if (!c->inited) return fail(c, GBH_ERR_STATE, "gbh_step before gbh_init");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = upload_params(c, p);
+    if (rc) return rc;
+    for (uint32_t s = 0; s < count; ++s) {
+        const int key = graph_key(c);
+        auto it = c->graphs.find(key);
+        if (it == c->graphs.end()) {
+            const int bin0 = c->bin, iin0 = c->iin;
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            rc = enqueue_step(c);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            c->bin = bin0;
+            c->iin = iin0;
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return fail(c, GBH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            cudaGraphExec_t ex = nullptr;
+            e = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(c, GBH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            it = c->graphs.emplace(key, ex).first;
+        }
+        CUDA_TRY(c, cudaGraphLaunch(it->second, c->stream));
+        // the step flips both the body buffers and the (morton, index) buffers
+        c->bin = 1 - c->bin;
+        c->iin = 1 - c->iin;
+    }
+    return GBH_OK;
+}
+
+int gbh_synchronize(gbh_ctx* c) {
+    if (!c) return fail(c, GBH_ERR_INVALID, "null context");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    uint32_t ew = 0;
+    CUDA_TRY(c, cudaMemcpy(&ew, &c->st->error_word, 4, cudaMemcpyDeviceToHost));
+    if (ew) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "device error word 0x%x", ew);
+        return fail(c, GBH_ERR_DEVICE, buf);
+    }
+    return GBH_OK;
+}
+
+int gbh_clear_error(gbh_ctx* c) {
+    if (!c) return GBH_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemsetAsync(&c->st->error_word, 0, 4, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->last_error.clear();
+    return GBH_OK;
+}
+
+// ---- read-back --------------------------------------------------------------
+
+static int read_dev(gbh_ctx* c, void* host, const void* dev, size_t bytes) {
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+static int write_dev(gbh_ctx* c, void* dev, const void* host, size_t bytes) {
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    CUDA_TRY(c, cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+#define RANGE_CHECK(c, host, count, offset, cap)                                                  \
+    do {                                                                                          \
+        if (!(c)) return GBH_ERR_INVALID;                                                         \
+        if (!(host) && (count)) return fail((c), GBH_ERR_INVALID, "null host buffer");            \
+        if ((uint64_t)(offset) + (count) > (cap)) return fail((c), GBH_ERR_INVALID, "range out of bounds"); \
+    } while (0)
+
+int gbh_read_bodies(gbh_ctx* c, uint32_t which, gbh_body* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    if (which > 1) return fail(c, GBH_ERR_INVALID, "which must be GBH_BODIES_IN or GBH_BODIES_OUT");
+    const gbh_body* src = c->bodies[which == GBH_BODIES_IN ? c->bin : 1 - c->bin];
+    return read_dev(c, host, src + offset, (size_t)count * sizeof(gbh_body));
+}
+
+int gbh_read_leaf_nodes(gbh_ctx* c, gbh_node* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return read_dev(c, host, c->leaf + offset, (size_t)count * sizeof(gbh_node));
+}
+
+int gbh_read_internal_nodes(gbh_ctx* c, gbh_node* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N > 1 ? c->N - 1 : 1);
+    return read_dev(c, host, c->internal + offset, (size_t)count * sizeof(gbh_node));
+}
+
+int gbh_read_sim_values(gbh_ctx* c, gbh_sim_values* host) {
+    if (!c || !host) return GBH_ERR_INVALID;
+    return read_dev(c, host, c->sim, sizeof(gbh_sim_values));
+}
+
+int gbh_read_index(gbh_ctx* c, uint32_t* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return read_dev(c, host, c->idx[c->iin] + offset, (size_t)count * 4);
+}
+
+int gbh_read_morton(gbh_ctx* c, uint64_t* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return read_dev(c, host, c->keys[c->iin] + offset, (size_t)count * 8);
+}
+
+int gbh_read_merge_tasks(gbh_ctx* c, uint32_t* host_pairs, uint32_t capacity, uint32_t* count) {
+    if (!c || !count) return GBH_ERR_INVALID;
+    uint32_t ht[2];
+    int rc = read_dev(c, ht, c->mq, 8);
+    if (rc) return rc;
+    const uint32_t m = ht[1] < c->N ? ht[1] : c->N;
+    *count = m;
+    const uint32_t k = m < capacity ? m : capacity;
+    if (k && host_pairs) return read_dev(c, host_pairs, c->mq->pairs, (size_t)k * 8);
+    return GBH_OK;
+}
+
+int gbh_read_accel(gbh_ctx* c, float* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return read_dev(c, host, c->accel + offset, (size_t)count * 16);
+}
+
+int gbh_read_stats(gbh_ctx* c, gbh_stats* s) {
+    if (!c || !s) return GBH_ERR_INVALID;
+    DevState st;
+    int rc = read_dev(c, &st, c->st, sizeof(st));
+    if (rc) return rc;
+    memset(s, 0, sizeof(*s));
+    s->interactions = st.interactions;
+    s->nodes_opened = st.opened;
+    s->mac_evaluations = st.mac_evals;
+    s->alive = st.n_new;
+    s->died = st.just_died;
+    s->merged = st.merged;
+    s->merge_tasks = st.merge_tasks;
+    s->merge_conflicts = st.merge_conflicts;
+    s->out_of_bounds = st.oob;
+    s->tree_height = st.tree_height;
+    s->max_stack = st.max_stack;
+    s->error_word = st.error_word;
+    return GBH_OK;
+}
+
+int gbh_device_ptrs(gbh_ctx* c, gbh_device_buffers* o) {
+    if (!c || !o) return GBH_ERR_INVALID;
+    o->bodies_in = c->bodies[c->bin];
+    o->bodies_out = c->bodies[1 - c->bin];
+    o->leaf_nodes = c->leaf;
+    o->internal_nodes = c->internal;
+    o->sim_values = c->sim;
+    o->morton_in = c->keys[c->iin];
+    o->index_in = c->idx[c->iin];
+    o->merge_tasks = c->mq;
+    return GBH_OK;
+}
+
+void* gbh_stream(gbh_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int gbh_write_sim_values(gbh_ctx* c, const gbh_sim_values* host) {
+    if (!c || !host) return GBH_ERR_INVALID;
+    return write_dev(c, c->sim, host, sizeof(gbh_sim_values));
+}
+
+int gbh_write_index(gbh_ctx* c, const uint32_t* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return write_dev(c, c->idx[c->iin] + offset, host, (size_t)count * 4);
+}
+
+int gbh_write_morton(gbh_ctx* c, const uint64_t* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    return write_dev(c, c->keys[c->iin] + offset, host, (size_t)count * 8);
+}
+
+// ---- stage entry points -------------------------------------------------------
+
+static int stage_common(gbh_ctx* c, const gbh_step_params* p) {
+    if (!c) return GBH_ERR_INVALID;
+    if (!c->inited) return fail(c, GBH_ERR_STATE, "stage call before gbh_init");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (p) return upload_params(c, p);
+    if (!c->params_valid) return fail(c, GBH_ERR_STATE, "stage call before any step parameters were given");
+    return GBH_OK;
+}
+
+#define STAGE_BODY(c, p, fn)          \
+    do {                              \
+        int rc_ = stage_common(c, p); \
+        if (rc_) return rc_;          \
+        rc_ = fn(c);                  \
+        if (rc_) return rc_;          \
+        return gbh_synchronize(c);    \
+    } while (0)
+
+int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_reset); }
+int gbh_stage_prepare(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_prepare); }
+int gbh_stage_sort(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_sort); }
+int gbh_stage_build(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_build); }
+int gbh_stage_fill(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_fill); }
+int gbh_stage_walk(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_walk); }
+int gbh_stage_merge(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_merge); }
+int gbh_stage_swap(gbh_ctx* c) {
+    if (!c) return GBH_ERR_INVALID;
+    return enqueue_swap(c);
+}
+
+int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM_STAGES]) {
+    int rc = stage_common(c, p);
+    if (rc) return rc;
+    if (!ms_out) return fail(c, GBH_ERR_INVALID, "ms_out is null");
+    cudaEvent_t ev[GBH_NUM_STAGES + 1];
+    for (int i = 0; i <= GBH_NUM_STAGES; ++i) CUDA_TRY(c, cudaEventCreate(&ev[i]));
+    CUDA_TRY(c, cudaEventRecord(ev[0], c->stream));
+    for (int s = 0; s < GBH_NUM_STAGES; ++s) {
+        rc = k_stages[s](c);
+        if (rc) break;
+        CUDA_TRY(c, cudaEventRecord(ev[s + 1], c->stream));
+    }
+    if (!rc) {
+        CUDA_TRY(c, cudaEventSynchronize(ev[GBH_NUM_STAGES]));
+        for (int s = 0; s < GBH_NUM_STAGES; ++s) CUDA_TRY(c, cudaEventElapsedTime(&ms_out[s], ev[s], ev[s + 1]));
+    }
+    for (int i = 0; i <= GBH_NUM_STAGES; ++i) cudaEventDestroy(ev[i]);
+    if (rc) return rc;
+    return gbh_synchronize(c);
+}
+
+int gbh_direct_sum(gbh_ctx* c, const gbh_step_params* p, const uint32_t* sample, uint32_t count, double* out) {
+    if (!c || !p || (!sample && count) || (!out && count)) return fail(c, GBH_ERR_INVALID, "null argument");
+    if (count == 0) return GBH_OK;
+    for (uint32_t i = 0; i < count; ++i)
+        if (sample[i] >= c->N) return fail(c, GBH_ERR_INVALID, "sample index out of range");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    gbh_sim_values sv;
+    int rc = read_dev(c, &sv, c->sim, sizeof(sv));
+    if (rc) return rc;
+    const uint32_t blocks = (count + 127) / 128;
+    uint32_t chunks = (152 * 16 + blocks - 1) / blocks;
+    if (chunks < 1) chunks = 1;
+    if (chunks > c->N) chunks = c->N;
+    uint32_t* d_sample = nullptr;
+    double *d_partial = nullptr, *d_out = nullptr;
+    CUDA_TRY(c, cudaMalloc(&d_sample, (size_t)count * 4));
+    CUDA_TRY(c, cudaMalloc(&d_partial, (size_t)chunks * count * 3 * 8));
+    CUDA_TRY(c, cudaMalloc(&d_out, (size_t)count * 3 * 8));
+    cudaError_t e = cudaMemcpyAsync(d_sample, sample, (size_t)count * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        launch_direct_sum(c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant, p->softening,
+                          d_partial, d_out, chunks, c->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, (size_t)count * 3 * 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_sample);
+    cudaFree(d_partial);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return fail(c, GBH_ERR_CUDA, std::string("direct sum: ") + cudaGetErrorString(e));
+    return GBH_OK;
+}
+
+}  // extern "C"

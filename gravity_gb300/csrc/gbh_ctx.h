@@ -1,0 +1,61 @@
+// gbh_ctx.h — the context object behind the opaque gbh_ctx handle.
+#pragma once
+
+#include <map>
+#include <string>
+
+#include "gbh_common.cuh"
+
+struct MacState;  // learned MAC buffers (k_mac.cu)
+
+struct gbh_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t N = 0;
+    uint32_t prep_tiles_cap = 0;
+    uint32_t sort_tiles_cap = 0;
+    gbh_units units{};
+    bool inited = false;
+
+    // one device arena holding every buffer below
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    gbh_body* bodies[2] = {nullptr, nullptr};
+    int bin = 0;  // bodies[bin] is BodiesIn
+    uint64_t* keys[2] = {nullptr, nullptr};
+    uint32_t* idx[2] = {nullptr, nullptr};
+    int iin = 0;  // keys[iin], idx[iin] are MortonIn / IndexIn
+    gbh_node* leaf = nullptr;
+    gbh_node* internal = nullptr;
+    WalkNode* wnode = nullptr;
+    float4* leaf_pm = nullptr;
+    float* leaf_rad = nullptr;
+    gbh_sim_values* sim = nullptr;
+    DevState* st = nullptr;
+    gbh_step_params* params_dev = nullptr;
+    MergeQueue* mq = nullptr;
+    unsigned long long* mkeys = nullptr;
+    uint32_t* locks = nullptr;
+    uint32_t* conflicts = nullptr;
+    float4* accel = nullptr;
+    uint32_t* tile_dead = nullptr;
+    float* tile_aabb = nullptr;
+    uint32_t* hist = nullptr;
+    uint32_t* bucket_base = nullptr;
+    uint32_t* lookback = nullptr;
+    size_t lookback_bytes = 0;
+
+    gbh_step_params params_host{};
+    bool params_valid = false;
+    uint32_t mac_mode = GBH_MAC_PLAIN;
+    bool mac_ready = false;
+    MacState* mac = nullptr;
+
+    std::map<int, cudaGraphExec_t> graphs;
+    std::string last_error;
+};
+
+StepBuffers ctx_buffers(const gbh_ctx* c);
+int enqueue_walk_learned(gbh_ctx* c);
+void mac_release(gbh_ctx* c);
+void sort_setup();

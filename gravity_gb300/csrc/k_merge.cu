@@ -1,0 +1,164 @@
+// k_merge.cu — merge resolution.
+//
+// Replaces mergeBodiesKernel (SH/compute/merge/bh_merge.comp:30-71): every
+// thread loops on an atomic queue head and try-locks both bodies, skipping a
+// task when a lock is taken, so the outcome depends on scheduling.
+//
+// Here the outcome is deterministic and equals the reference run with a
+// single thread in the walk's emission order (slot-major, then depth-first
+// order inside a body's walk), a schedule under which no try-lock fails:
+//   1. count how many tasks touch each body (the lock words double as counters);
+//   2. a task whose two bodies appear in no other task commutes with every
+//      other task and is applied at once, in parallel;
+//   3. the remaining (conflicting) tasks are ordered by their emission key in
+//      one block (bitonic sort in shared memory) and applied by one thread;
+//   4. the lock words are cleared again.
+#include "gbh_common.cuh"
+
+#define MERGE_CONFLICT_CAP 4096
+#define MERGE_SORT_THREADS 1024
+
+// mergeBodies, bh_merge.comp:5-22
+__device__ __forceinline__ void merge_two(float4& p1, float4& v1, const float4 p2, const float4 v2) {
+    const float m1 = p1.w, m2 = p2.w;
+    const float M = m1 + m2;
+    if (M == 0.0f) {
+        p1 = make_float4(0.f, 0.f, 0.f, 0.f);
+        v1 = p1;
+        return;
+    }
+    if (m1 == 0.0f) {
+        p1 = p2;
+        v1 = v2;
+        return;
+    }
+    if (m2 == 0.0f) return;
+    float4 np, nv;
+    np.x = (p1.x * m1 + p2.x * m2) / M;
+    np.y = (p1.y * m1 + p2.y * m2) / M;
+    np.z = (p1.z * m1 + p2.z * m2) / M;
+    np.w = M;
+    nv.x = (v1.x * m1 + v2.x * m2) / M;
+    nv.y = (v1.y * m1 + v2.y * m2) / M;
+    nv.z = (v1.z * m1 + v2.z * m2) / M;
+    nv.w = (m1 + m2) / (m1 / v1.w + m2 / v2.w);
+    p1 = np;
+    v1 = nv;
+}
+
+// apply task (a, b) on the output bodies; returns true when merged
+__device__ __forceinline__ bool apply_task(gbh_body* dst, uint32_t a, uint32_t c) {
+    if (a == c) return false;
+    float4 p1 = ld_pos_mass(dst, a), v1 = ld_vel_density(dst, a);
+    const float4 p2 = ld_pos_mass(dst, c), v2 = ld_vel_density(dst, c);
+    if (p1.w == 0.0f || p2.w == 0.0f) return false;
+    merge_two(p1, v1, p2, v2);
+    st_body(dst, a, p1, v1);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    st_body(dst, c, z, z);
+    return true;
+}
+
+__global__ void k_merge_count(StepBuffers b) {
+    const uint32_t M = min(b.mq->tail, b.N);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        const uint2 pr = b.mq->pairs[t];
+        atomicAdd(&b.locks[pr.x], 1u);
+        atomicAdd(&b.locks[pr.y], 1u);
+    }
+}
+
+__global__ void k_merge_apply(StepBuffers b) {
+    const uint32_t M = min(b.mq->tail, b.N);
+    uint32_t merged = 0;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        const uint2 pr = b.mq->pairs[t];
+        if (b.locks[pr.x] == 1u && b.locks[pr.y] == 1u) {
+            merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+        } else {
+            const uint32_t slot = atomicAdd(&b.st->merge_conflicts, 1u);
+            b.conflicts[slot] = t;
+        }
+    }
+    if (merged) atomicAdd(&b.st->merged, merged);
+}
+
+__global__ __launch_bounds__(MERGE_SORT_THREADS) void k_merge_conflicts(StepBuffers b) {
+    __shared__ unsigned long long s_key[MERGE_CONFLICT_CAP];
+    __shared__ uint32_t s_task[MERGE_CONFLICT_CAP];
+    const uint32_t C = b.st->merge_conflicts;
+    if (threadIdx.x == 0) b.st->merge_tasks = min(b.mq->tail, b.N);
+    if (C == 0) return;
+    if (C > MERGE_CONFLICT_CAP) {
+        // too many to order in one block: apply in list order (still a valid
+        // single-thread schedule of the reference, but not the emission order)
+        if (threadIdx.x == 0) {
+            set_error(b.st, GBH_DEVERR_MERGE_OVERFLOW);
+            uint32_t merged = 0;
+            for (uint32_t k = 0; k < C; ++k) {
+                const uint2 pr = b.mq->pairs[b.conflicts[k]];
+                merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+            }
+            b.st->merged += merged;
+        }
+        return;
+    }
+    uint32_t P = 1;
+    while (P < C) P <<= 1;
+    for (uint32_t k = threadIdx.x; k < P; k += blockDim.x) {
+        if (k < C) {
+            const uint32_t t = b.conflicts[k];
+            s_key[k] = b.mkeys[t];
+            s_task[k] = t;
+        } else {
+            s_key[k] = ~0ull;
+            s_task[k] = GBH_NONE;
+        }
+    }
+    __syncthreads();
+    // bitonic sort by emission key
+    for (uint32_t size = 2; size <= P; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t k = threadIdx.x; k < P; k += blockDim.x) {
+                const uint32_t j = k ^ stride;
+                if (j > k) {
+                    const bool up = (k & size) == 0;
+                    const unsigned long long a = s_key[k], c = s_key[j];
+                    if ((a > c) == up) {
+                        s_key[k] = c;
+                        s_key[j] = a;
+                        const uint32_t tt = s_task[k];
+                        s_task[k] = s_task[j];
+                        s_task[j] = tt;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        uint32_t merged = 0;
+        for (uint32_t k = 0; k < C; ++k) {
+            const uint2 pr = b.mq->pairs[s_task[k]];
+            merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+        }
+        b.st->merged += merged;
+    }
+}
+
+__global__ void k_merge_clear(StepBuffers b) {
+    const uint32_t M = min(b.mq->tail, b.N);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        const uint2 pr = b.mq->pairs[t];
+        b.locks[pr.x] = 0u;
+        b.locks[pr.y] = 0u;
+    }
+}
+
+void launch_merge(const StepBuffers& b, cudaStream_t s) {
+    const uint32_t blocks = 152 * 4;
+    k_merge_count<<<blocks, 256, 0, s>>>(b);
+    k_merge_apply<<<blocks, 256, 0, s>>>(b);
+    k_merge_conflicts<<<1, MERGE_SORT_THREADS, 0, s>>>(b);
+    k_merge_clear<<<blocks, 256, 0, s>>>(b);
+}

@@ -1,0 +1,209 @@
+// k_sort.cu — stable LSD radix sort of (63-bit Morton key, u32 body index).
+//
+// Replaces radixSort (src/main/java/com/grumbo/simulation/BarnesHut.java:358-448)
+// and its four kernels (SH/compute/radix/bh_radix.comp:12-166): 16 passes of
+// 4-bit digits, each pass histogram -> per-bucket scan -> global scan ->
+// scatter with an O(256) serial rank loop.  Any stable LSD sort of the same
+// keys yields the same permutation, so this is a onesweep sort (Adinets &
+// Merrill 2022): 8 passes of 8-bit digits, one kernel per pass.
+//   * The eight digit histograms are accumulated by the encode pass
+//     (k_prep_scatter) and scanned here once (k_sort_scan).
+//   * Each pass kernel takes a tile ticket, ranks its keys with warp
+//     match-any, publishes the tile's digit counts, resolves its global digit
+//     offsets with a decoupled look-back (bounded spin, error word on
+//     timeout), stages keys digit-ordered in shared memory and writes them out
+//     with coalesced runs.
+#include "gbh_common.cuh"
+
+#define LB_FLAG_AGG 0x40000000u
+#define LB_FLAG_INC 0x80000000u
+#define LB_COUNT_MASK 0x3FFFFFFFu
+#define LB_SPIN_LIMIT (1u << 22)
+
+__global__ void k_sort_scan(StepBuffers b) {
+    // one block per pass: exclusive scan of the 256 digit counts
+    const uint32_t p = blockIdx.x;
+    const uint32_t d = threadIdx.x;
+    const uint32_t v = b.hist[p * SORT_RADIX + d];
+    __shared__ uint32_t s_w[SORT_RADIX / 32];
+    const uint32_t lane = lane_id(), w = d >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    uint32_t off = 0;
+    for (uint32_t i = 0; i < w; ++i) off += s_w[i];
+    b.bucket_base[p * SORT_RADIX + d] = off + x - v;
+}
+
+struct SortSmem {
+    uint32_t warp_hist[SORT_THREADS / 32][SORT_RADIX + 1];  // +1: sentinel bucket of out-of-range items
+    uint32_t block_excl[SORT_RADIX + 1];
+    uint32_t delta[SORT_RADIX];
+    uint32_t warp_tot[SORT_THREADS / 32];
+    uint32_t tile;
+    unsigned long long keys[SORT_TILE];
+    uint32_t vals[SORT_TILE];
+};
+
+__global__ __launch_bounds__(SORT_THREADS, 2) void k_sort_pass(StepBuffers b, uint32_t pass, const uint64_t* __restrict__ kin,
+                                                               const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+                                                               uint32_t* __restrict__ vout) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SortSmem& S = *reinterpret_cast<SortSmem*>(smem_raw);
+    const uint32_t n = b.st->n_new;
+    const uint32_t shift = SORT_BITS * pass;
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) S.tile = atomicAdd(&b.st->sort_tiles[pass], 1u);
+    for (uint32_t i = threadIdx.x; i < (SORT_THREADS / 32) * (SORT_RADIX + 1); i += SORT_THREADS)
+        (&S.warp_hist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = S.tile;
+    const uint32_t base = tile * SORT_TILE;
+    if (base >= n) return;
+    uint32_t* lb = b.lookback + ((size_t)pass * b.sort_tiles_cap) * SORT_RADIX;
+
+    // load: warp w owns slots [base + w*32*ITEMS, +32*ITEMS), item i of lane l at +i*32+l
+    const uint32_t seg = base + w * 32 * SORT_ITEMS;
+    uint64_t key[SORT_ITEMS];
+    uint32_t val[SORT_ITEMS];
+    uint32_t rank[SORT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t pos = seg + i * 32 + lane;
+        if (pos < n) {
+            key[i] = kin[pos];
+            val[i] = vin[pos];
+        } else {
+            key[i] = ~0ull;
+            val[i] = 0;
+        }
+    }
+    // warp-level stable ranking, item rounds in slot order
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t pos = seg + i * 32 + lane;
+        const uint32_t dig = pos < n ? (uint32_t)((key[i] >> shift) & 0xFF) : SORT_RADIX;
+        const uint32_t peers = __match_any_sync(0xffffffffu, dig);
+        const uint32_t leader = __ffs(peers) - 1;
+        const uint32_t before = __popc(peers & lanemask_lt());
+        const uint32_t cnt = __popc(peers);
+        const uint32_t prev = S.warp_hist[w][dig];
+        __syncwarp();
+        if (lane == leader) S.warp_hist[w][dig] = prev + cnt;
+        __syncwarp();
+        rank[i] = prev + before;
+    }
+    __syncthreads();
+    // thread d: exclusive prefix of digit d over warps, tile total
+    const uint32_t d = threadIdx.x;
+    uint32_t total = 0;
+#pragma unroll
+    for (int ww = 0; ww < SORT_THREADS / 32; ++ww) {
+        const uint32_t c = S.warp_hist[ww][d];
+        S.warp_hist[ww][d] = total;
+        total += c;
+    }
+    // publish this tile's count for digit d (inclusive when it is the first tile)
+    volatile uint32_t* my = lb + (size_t)tile * SORT_RADIX + d;
+    if (tile == 0) {
+        *my = LB_FLAG_INC | total;
+    } else {
+        *my = LB_FLAG_AGG | total;
+    }
+    // block exclusive scan of totals over digits -> block_excl
+    {
+        uint32_t x = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) S.warp_tot[w] = x;
+        __syncthreads();
+        uint32_t off = 0;
+        for (uint32_t i = 0; i < w; ++i) off += S.warp_tot[i];
+        S.block_excl[d] = off + x - total;
+        if (d == 0) S.block_excl[SORT_RADIX] = 0;
+    }
+    // decoupled look-back for digit d
+    uint32_t prefix = 0;
+    if (tile > 0) {
+        int32_t j = (int32_t)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            const uint32_t v = *(volatile uint32_t*)(lb + (size_t)j * SORT_RADIX + d);
+            if (v & LB_FLAG_INC) {
+                prefix += v & LB_COUNT_MASK;
+                break;
+            }
+            if (v & LB_FLAG_AGG) {
+                prefix += v & LB_COUNT_MASK;
+                --j;
+                continue;
+            }
+            if (++spins > LB_SPIN_LIMIT) {
+                set_error(b.st, GBH_DEVERR_SORT_LOOKBACK);
+                break;
+            }
+            __nanosleep(20);
+        }
+        *my = LB_FLAG_INC | (prefix + total);
+    }
+    S.delta[d] = b.bucket_base[pass * SORT_RADIX + d] + prefix - S.block_excl[d];
+    __syncthreads();
+    // stage digit-ordered in shared memory
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t pos = seg + i * 32 + lane;
+        if (pos < n) {
+            const uint32_t dig = (uint32_t)((key[i] >> shift) & 0xFF);
+            const uint32_t local = S.block_excl[dig] + S.warp_hist[w][dig] + rank[i];
+            S.keys[local] = key[i];
+            S.vals[local] = val[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t valid = min((uint32_t)SORT_TILE, n - base);
+    bool bad = false;
+    for (uint32_t j = threadIdx.x; j < valid; j += SORT_THREADS) {
+        const uint64_t k = S.keys[j];
+        const uint32_t dig = (uint32_t)((k >> shift) & 0xFF);
+        const uint32_t dst = S.delta[dig] + j;
+        if (dst < n) {  // holds whenever the digit histograms describe these keys
+            kout[dst] = k;
+            vout[dst] = S.vals[j];
+        } else {
+            bad = true;
+        }
+    }
+    if (bad) set_error(b.st, GBH_DEVERR_SORT_LOOKBACK);
+}
+
+void sort_setup() {
+    cudaFuncSetAttribute(k_sort_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+}
+
+void launch_sort(const StepBuffers& b, cudaStream_t s) {
+    const size_t smem = sizeof(SortSmem);
+    k_sort_scan<<<SORT_PASSES, SORT_RADIX, 0, s>>>(b);
+    // keys/index of the live bodies are in the *_in buffers (the compaction
+    // swap already happened); 8 ping-pong passes through *_out end there again
+    const uint64_t* kin = b.keys_in;
+    const uint32_t* vin = b.idx_in;
+    uint64_t* kt = b.keys_out;
+    uint32_t* vt = b.idx_out;
+    for (uint32_t p = 0; p < SORT_PASSES; ++p) {
+        k_sort_pass<<<b.sort_tiles_cap, SORT_THREADS, smem, s>>>(b, p, kin, vin, kt, vt);
+        const uint64_t* nk = kt;
+        const uint32_t* nv = vt;
+        kt = const_cast<uint64_t*>(kin);
+        vt = const_cast<uint32_t*>(vin);
+        kin = nk;
+        vin = nv;
+    }
+}

@@ -1,0 +1,313 @@
+/*
+ * gbh.h — C ABI of the GB300-native Barnes–Hut step.
+ *
+ * This header is the drop-in boundary for the per-step pipeline of the
+ * gkane1234/gravity simulator.  A Java host (Panama FFM or JNI), a Python host
+ * (ctypes) or C/C++ code binds these entry points; nothing in the signatures is
+ * a torch or CUDA-runtime type (streams are passed as opaque `void*`).
+ *
+ * Reference interface replaced (paths inside the reference project):
+ *   - BarnesHut.init()/step()          src/main/java/com/grumbo/simulation/BarnesHut.java:99-173
+ *   - GPU.initGPU()/uploadPlanetsData  src/main/java/com/grumbo/gpu/GPU.java:172-188, 1166-1196
+ *   - the SSBO binding table           src/main/java/com/grumbo/gpu/SSBO.java:40-55,
+ *                                      src/main/resources/shaders/common/common.glsl:80-120
+ *   - uniforms of the step             common.glsl:126-158, GPU.java:402-498
+ *
+ * Layouts are byte-identical to the reference's std430 SSBO layouts so buffers
+ * read back from this library can be handed to code written for the reference.
+ *
+ * Error convention: every entry point returns an int status (GBH_OK == 0,
+ * negative == error class).  gbh_last_error(ctx) returns a human-readable
+ * message for the last failing call on that context; gbh_last_error(NULL)
+ * returns the message of the last failing gbh_create on this thread.  No C++
+ * exception crosses this boundary.
+ *
+ * Threading: one context per host thread; calls on one context must be
+ * serialised by the caller (the reference runs everything on its single GL
+ * thread, GPUSimulation.java:379-384).  All device work of a context runs on
+ * the context's own CUDA stream.
+ */
+#ifndef GBH_H
+#define GBH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBH_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define GBH_OK 0
+#define GBH_ERR_INVALID (-1)  /* bad argument (null pointer, size out of range, bad enum) */
+#define GBH_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define GBH_ERR_OOM (-3)      /* device allocation failed */
+#define GBH_ERR_DEVICE (-4)   /* a kernel raised the device error word (see gbh_stats.error_word) */
+#define GBH_ERR_STATE (-5)    /* call out of order (e.g. step before init) */
+#define GBH_ERR_UNSUPPORTED (-6)
+
+/* ---- device error word bits (gbh_stats.error_word) ------------------------ */
+#define GBH_DEVERR_SORT_LOOKBACK 0x1u   /* onesweep look-back spin gave up (bounded wait) */
+#define GBH_DEVERR_FILL_SPIN 0x2u       /* reserved: bottom-up fill never spins, kept for ABI stability */
+#define GBH_DEVERR_WALK_STACK 0x4u      /* a tree walk needed more stack than GBH_WALK_STACK */
+#define GBH_DEVERR_MERGE_OVERFLOW 0x8u  /* more conflicting merge tasks than one block can order */
+#define GBH_DEVERR_TREE_HEIGHT 0x10u    /* tree height above 64 (the reference fills only 64 levels) */
+#define GBH_DEVERR_MAC_FRONTIER 0x20u   /* learned walk frontier overflow */
+
+/* ---- enums mirroring the reference uniforms ------------------------------ */
+/* mergingCollisionOrNeither (common.glsl:133-140, defaultProperties.json order) */
+#define GBH_MODE_NEITHER 0u
+#define GBH_MODE_MERGE 1u
+#define GBH_MODE_COLLISION 2u
+/* staticOrDynamic (common.glsl:146-149) */
+#define GBH_BOUNDS_STATIC 0u
+#define GBH_BOUNDS_DYNAMIC 1u
+/* acceptance criterion of the walk (new in this library) */
+#define GBH_MAC_PLAIN 0u    /* reference rule: (longest AABB side / 2) * invDist < theta, per body */
+#define GBH_MAC_LEARNED 1u  /* learned MLP criterion, one decision per (32-body group, node) */
+#define GBH_MAC_GROUP 2u    /* group theta rule used as the learned criterion's ablation */
+/* precision form (new in this library) */
+#define GBH_PRECISION_FP32 0u     /* reference arithmetic */
+#define GBH_PRECISION_COMPENSATED 1u /* FP64 drift + compensated FP32 force sums */
+
+/* step flags */
+#define GBH_FLAG_STORE_ACCEL 0x1u  /* keep each body's walk acceleration (gbh_read_accel) */
+
+/* ---- buffers, byte-identical to the reference std430 layouts -------------- */
+
+/* struct Body, common.glsl:25-29 (32 bytes). Empty <=> pos_mass[3] == 0. */
+typedef struct gbh_body {
+    float pos_mass[4];    /* x, y, z, mass */
+    float vel_density[4]; /* vx, vy, vz, density */
+} gbh_body;
+
+/* struct Node, common.glsl:40-58 (80 bytes).  Leaves are indexed by sorted
+ * position; internal node ids are offset by initialNumBodies; a leaf has
+ * child_a == 0xFFFFFFFF. */
+typedef struct gbh_node {
+    float com_mass[4];      /* @0  centre of mass xyz, mass */
+    float aabb[6];          /* @16 min xyz, max xyz */
+    uint32_t child_a;       /* @40 */
+    uint32_t child_b;       /* @44 */
+    uint32_t node_depth;    /* @48 height above the deepest leaf after the fill */
+    uint32_t bodies_contained; /* @52 */
+    uint32_t ready_children;   /* @56 0xFFFFFFFF once filled */
+    uint32_t parent_id;        /* @60 0xFFFFFFFF for the root */
+    float avg_color[4];        /* @64 mass-weighted star colour (rgb), w unused */
+} gbh_node;
+
+/* buffer SimulationValues, common.glsl:86-88, with std430 offsets (896 bytes
+ * as allocated by GPU.java:1096-1143). */
+typedef struct gbh_sim_values {
+    uint32_t num_bodies;         /* @0 live bodies */
+    uint32_t initial_num_bodies; /* @4 capacity */
+    uint32_t just_died;          /* @8 */
+    uint32_t merged;             /* @12 (never incremented by the reference) */
+    uint32_t out_of_bounds;      /* @16 cumulative count of bodies killed out of bounds */
+    uint32_t relative_to;        /* @20 */
+    uint32_t pad1, pad2;         /* @24 */
+    float bounds_min[3];         /* @32 */
+    uint32_t pad_min;            /* @44 */
+    float bounds_max[3];         /* @48 */
+    uint32_t pad_max;            /* @60 */
+    float unit_mass;             /* @64 */
+    float unit_density;          /* @68 */
+    float unit_len;              /* @72 */
+    float unit_time;             /* @76 */
+    float camera_scale;          /* @80 */
+    float gravitational_constant;/* @84 */
+    float body_length_constant;  /* @88 bodyLengthInSimulationLengthsConstant */
+    uint32_t uint_debug[100];    /* @92 uint_debug[0] = internal nodes opened by the walk */
+    float float_debug[100];      /* @492 */
+    uint32_t tail_pad;           /* @892 */
+} gbh_sim_values;
+
+/* UnitSet (common.glsl:61-70, UnitSet.java:242-245).  G and the body length
+ * constant are derived from these in FP32 like common.glsl:346-360 unless
+ * gravitational_constant > 0, which then overrides the derived G. */
+typedef struct gbh_units {
+    float mass;
+    float density;
+    float len;
+    float time;
+    float camera_scale;
+    float gravitational_constant; /* > 0: use this G directly */
+} gbh_units;
+
+/* The step's uniforms (common.glsl:126-158). */
+typedef struct gbh_step_params {
+    float dt;
+    float theta;
+    float softening;   /* added to r.r directly: this is eps^2 (bh_force.comp:27-32) */
+    float elasticity;
+    float restitution; /* the reference hard-codes 0.2 (GPU.java:442-446) */
+    uint32_t merging_collision_or_neither; /* GBH_MODE_* */
+    uint32_t static_or_dynamic;            /* GBH_BOUNDS_* */
+    uint32_t wrap_around;                  /* static bounds: wrap instead of kill */
+    gbh_units units;   /* units.mass == 0 keeps the current units (bh_update.comp:22-25) */
+    uint32_t mac_mode;        /* GBH_MAC_* */
+    uint32_t precision_mode;  /* GBH_PRECISION_* */
+    float mac_tolerance;      /* learned MAC: accept when predicted log10 error < this */
+    uint32_t flags;           /* GBH_FLAG_* */
+} gbh_step_params;
+
+/* Per-step counters (read with gbh_read_stats). */
+typedef struct gbh_stats {
+    uint64_t interactions;   /* body-node force evaluations (accepted nodes + leaves) */
+    uint64_t nodes_opened;   /* body-node openings (equals sim.uint_debug[0] when it fits) */
+    uint64_t mac_evaluations;/* learned/group walk: (group, node) criterion evaluations */
+    uint32_t alive;          /* live bodies after compaction */
+    uint32_t died;           /* bodies removed by this step's compaction */
+    uint32_t merged;         /* merge tasks applied */
+    uint32_t merge_tasks;    /* merge tasks emitted by the walk */
+    uint32_t merge_conflicts;/* tasks that shared a body with another task */
+    uint32_t out_of_bounds;  /* bodies killed out of bounds in this step */
+    uint32_t tree_height;    /* height of the root */
+    uint32_t max_stack;      /* deepest walk stack seen */
+    uint32_t error_word;     /* GBH_DEVERR_* bits, sticky until gbh_clear_error */
+    uint32_t pad;
+} gbh_stats;
+
+/* Device pointers of the live buffers, for headless consumers that replace the
+ * reference's render shaders reading the same SSBOs (nodeglow.vert, regions.vert,
+ * impostor.vert).  Valid until the next gbh_step (body/index buffers swap). */
+typedef struct gbh_device_buffers {
+    void* bodies_in;      /* gbh_body[initial_num_bodies] (current state) */
+    void* bodies_out;
+    void* leaf_nodes;     /* gbh_node[initial_num_bodies] */
+    void* internal_nodes; /* gbh_node[initial_num_bodies - 1] */
+    void* sim_values;     /* gbh_sim_values */
+    void* morton_in;      /* uint64_t[initial_num_bodies] sorted keys */
+    void* index_in;       /* uint32_t[initial_num_bodies] sorted body indices */
+    void* merge_tasks;    /* uint32_t head, tail, then uint32_t[2] pairs */
+} gbh_device_buffers;
+
+typedef struct gbh_ctx gbh_ctx;
+
+/* ---- lifecycle ----------------------------------------------------------- */
+
+/* GPU.initGPU (GPU.java:172-358): allocate every buffer for `initial_num_bodies`
+ * bodies on `device` and write SimulationValues like GPU.packValues
+ * (GPU.java:1096-1143).  bounds = {minx, miny, minz, maxx, maxy, maxz}. */
+int gbh_create(gbh_ctx** out, uint32_t initial_num_bodies, const float bounds[6],
+               const gbh_units* units, int device);
+int gbh_destroy(gbh_ctx* ctx);
+
+/* GPU.uploadPlanetsData (GPU.java:1166-1196): copy `count` bodies into the
+ * current body buffer starting at body `offset` (chunked uploads allowed). */
+int gbh_upload_bodies(gbh_ctx* ctx, const gbh_body* host, uint32_t count, uint32_t offset);
+
+/* BarnesHut.init (BarnesHut.java:170-173, bh_init.comp:10-27): identity index,
+ * derive G and the body length constant. */
+int gbh_init(gbh_ctx* ctx);
+
+/* BarnesHut.step (BarnesHut.java:99-164): one full step, launched as one CUDA
+ * graph on the context stream.  Asynchronous; errors raised by kernels are
+ * reported by the next synchronising call (read_* / gbh_synchronize). */
+int gbh_step(gbh_ctx* ctx, const gbh_step_params* params);
+/* `count` steps back to back with the same parameters. */
+int gbh_step_n(gbh_ctx* ctx, const gbh_step_params* params, uint32_t count);
+
+/* Wait for the context stream and return GBH_ERR_DEVICE if the device error
+ * word is non-zero. */
+int gbh_synchronize(gbh_ctx* ctx);
+int gbh_clear_error(gbh_ctx* ctx);
+
+/* ---- read-back (synchronous; host buffers are caller-owned) --------------- */
+#define GBH_BODIES_IN 0u
+#define GBH_BODIES_OUT 1u
+int gbh_read_bodies(gbh_ctx* ctx, uint32_t which, gbh_body* host, uint32_t count, uint32_t offset);
+int gbh_read_leaf_nodes(gbh_ctx* ctx, gbh_node* host, uint32_t count, uint32_t offset);
+int gbh_read_internal_nodes(gbh_ctx* ctx, gbh_node* host, uint32_t count, uint32_t offset);
+int gbh_read_sim_values(gbh_ctx* ctx, gbh_sim_values* host);
+int gbh_read_index(gbh_ctx* ctx, uint32_t* host, uint32_t count, uint32_t offset);
+int gbh_read_morton(gbh_ctx* ctx, uint64_t* host, uint32_t count, uint32_t offset);
+/* merge tasks emitted by the last walk: pairs (body, other); returns the count */
+int gbh_read_merge_tasks(gbh_ctx* ctx, uint32_t* host_pairs, uint32_t capacity, uint32_t* count);
+/* walk acceleration per body index (needs GBH_FLAG_STORE_ACCEL): float[4] per body */
+int gbh_read_accel(gbh_ctx* ctx, float* host_xyzw, uint32_t count, uint32_t offset);
+int gbh_read_stats(gbh_ctx* ctx, gbh_stats* host);
+int gbh_device_ptrs(gbh_ctx* ctx, gbh_device_buffers* out);
+/* opaque cudaStream_t of the context */
+void* gbh_stream(gbh_ctx* ctx);
+
+/* ---- write-back, for tests and checkpoint/resume -------------------------- */
+int gbh_write_sim_values(gbh_ctx* ctx, const gbh_sim_values* host);
+int gbh_write_index(gbh_ctx* ctx, const uint32_t* host, uint32_t count, uint32_t offset);
+int gbh_write_morton(gbh_ctx* ctx, const uint64_t* host, uint32_t count, uint32_t offset);
+
+/* ---- stage entry points (eager launches, for parity tests and profiling) ---
+ * Together, in this order, they are exactly one gbh_step:
+ *   reset -> prepare -> sort -> build -> fill -> walk -> merge -> swap.   */
+/* bh_update.comp:10-28 (resetValues, BarnesHut.java:193-212) */
+int gbh_stage_reset(gbh_ctx* ctx, const gbh_step_params* params);
+/* partitionDeadBodies + swap + decrementDeadBodies + updateBounds +
+ * generateMortonCodes (BarnesHut.java:114-131; bh_dead.comp, bh_update.comp:29-34,
+ * bh_morton.comp), fused into one pass over the index */
+int gbh_stage_prepare(gbh_ctx* ctx, const gbh_step_params* params);
+/* radixSort (BarnesHut.java:358-448; bh_radix.comp) over the live keys */
+int gbh_stage_sort(gbh_ctx* ctx);
+/* buildBinaryRadixTree (BarnesHut.java:453-469; bh_tree.comp:43-133) */
+int gbh_stage_build(gbh_ctx* ctx);
+/* computeCOMAndLocation (BarnesHut.java:474-535; bh_tree.comp:140-259) */
+int gbh_stage_fill(gbh_ctx* ctx);
+/* computeForce (BarnesHut.java:540-558; bh_force.comp:40-142) */
+int gbh_stage_walk(gbh_ctx* ctx, const gbh_step_params* params);
+/* mergeBodies (BarnesHut.java:563-579; bh_merge.comp:30-71) */
+int gbh_stage_merge(gbh_ctx* ctx, const gbh_step_params* params);
+/* GPU.swapBodyBuffers (GPU.java:1060-1066) */
+int gbh_stage_swap(gbh_ctx* ctx);
+
+/* ---- profiling (the reference's debug-mode per-stage timers,
+ *      BarnesHut.java:628-682, as CUDA events) ---------------------------- */
+#define GBH_NUM_STAGES 8
+/* Run one step as eager stage launches with CUDA events between stages and
+ * return per-stage milliseconds in stage order (reset, prepare, sort, build,
+ * fill, walk, merge, swap). */
+int gbh_step_profiled(gbh_ctx* ctx, const gbh_step_params* params, float ms_out[GBH_NUM_STAGES]);
+
+/* ---- accuracy judge -------------------------------------------------------
+ * Direct-sum accelerations for `count` sampled body indices against every live
+ * body of the current state (terms in FP32, sums compensated in double-float).
+ * out: double[3*count].  Uses G, softening from `params`. */
+int gbh_direct_sum(gbh_ctx* ctx, const gbh_step_params* params, const uint32_t* sample,
+                   uint32_t count, double* out_accel);
+
+/* ---- learned multipole-acceptance criterion -------------------------------- */
+#define GBH_MAC_FEATURES 12
+#define GBH_MAC_HIDDEN 32
+/* number of floats in the parameter vector: W1[32x12], b1[32], W2[32x32], b2[32], w3[32], b3[1] */
+#define GBH_MAC_NUM_PARAMS (32 * 12 + 32 + 32 * 32 + 32 + 32 + 1)
+int gbh_mac_set_weights(gbh_ctx* ctx, const float* params, uint32_t count);
+int gbh_mac_get_weights(gbh_ctx* ctx, float* params, uint32_t count);
+/* Sample (32-body group, node) pairs from the current tree, compute their
+ * features and labels (log10 of the relative error of accepting the node's
+ * monopole against its exact subtree sum, max over the group) into device
+ * buffers owned by the context.  Returns the number of pairs written. */
+int gbh_mac_generate(gbh_ctx* ctx, const gbh_step_params* params, uint32_t max_pairs,
+                     uint64_t seed, uint32_t* out_count);
+int gbh_mac_read_pairs(gbh_ctx* ctx, float* features, float* labels, uint32_t count, uint32_t offset);
+int gbh_mac_write_pairs(gbh_ctx* ctx, const float* features, const float* labels, uint32_t count);
+/* Train the MLP on the stored pairs with Adam (hand-written forward, backward
+ * and Adam kernels; BF16 tensor-core matmuls, FP32 master weights).
+ * losses: per-epoch mean loss (may be NULL). */
+int gbh_mac_train(gbh_ctx* ctx, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                  float* losses);
+/* Forward + backward of one batch (no update) for gradient checks:
+ * features[count*12], labels[count] in host memory; grad[GBH_MAC_NUM_PARAMS]. */
+int gbh_mac_loss_grad(gbh_ctx* ctx, const float* features, const float* labels, uint32_t count,
+                      float* loss, float* grad);
+/* Inference on host features: out[count] predicted log10 error. */
+int gbh_mac_predict(gbh_ctx* ctx, const float* features, uint32_t count, float* out);
+
+/* ---- library info ---------------------------------------------------------- */
+int gbh_abi_version(void);
+const char* gbh_last_error(gbh_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBH_H */

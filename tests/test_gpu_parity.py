@@ -1,0 +1,263 @@
+"""Parity of the sm_103a step against the CPU oracle, through the C ABI.
+
+Integer/index outputs (compaction order, Morton keys, sort permutation, tree
+topology) must be bit-exact; the fill's FP32 values are bit-exact too (same
+operations, no FMA); accelerations must match within 1e-5 median relative
+error (GLSL inversesqrt is rsqrtf on the GPU and 1/sqrtf in the oracle).
+"""
+import numpy as np
+import pytest
+
+from gravity_gb300 import abi
+from gravity_gb300 import BarnesHut
+
+from .helpers import bounds_of, make_pair, plummer_case, rel_err, sim_bounds
+
+pytestmark = pytest.mark.gpu
+
+ACCEL_MEDIAN_TOL = 1e-5
+
+
+def _prepare_both(g, o, p):
+    g.stage_reset(p)
+    o.stage_reset(p)
+    g.stage_prepare(p)
+    o.stage_prepare(p)
+
+
+@pytest.mark.parametrize("dynamic", [True, False])
+@pytest.mark.parametrize("n,dead,nans,outl", [(4096, 0.0, 0, 0), (5000, 0.1, 3, 5), (65536, 0.02, 0, 20), (1, 0.0, 0, 0), (2, 0.0, 0, 0), (2049, 0.5, 0, 0)])
+def test_prepare_bit_exact(gbh_lib, oracle_mod, n, dead, nans, outl, dynamic):
+    b = plummer_case(n, seed=n, dead_frac=dead, nan_count=nans, outliers=outl)
+    bounds = bounds_of(b) if n > 1 else np.array([-1, -1, -1, 1, 1, 1], np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds)
+    p = abi.step_params(bounds=abi.BOUNDS_DYNAMIC if dynamic else abi.BOUNDS_STATIC)
+    _prepare_both(g, o, p)
+    sg, so = g.read_sim_values(), o.read_sim_values()
+    assert sg.num_bodies == so.num_bodies
+    assert sg.just_died == so.just_died == 0
+    assert np.array_equal(sim_bounds(sg), sim_bounds(so))
+    nl = so.num_bodies
+    n_old = n
+    assert np.array_equal(g.read_index()[:n_old], o.read_index()[:n_old])
+    assert np.array_equal(g.read_morton()[:nl], o.read_morton()[:nl])
+    # dead bodies zeroed in both buffers
+    for w in (abi.BODIES_IN, abi.BODIES_OUT):
+        assert np.array_equal(g.read_bodies(w).view(np.uint32), o.read_bodies(w).view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [2, 3, 1000, 4096, 70000, 262144])
+def test_sort_permutation_bit_exact(gbh_lib, oracle_mod, n):
+    b = plummer_case(n, seed=7 + n)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds_of(b))
+    p = abi.step_params()
+    _prepare_both(g, o, p)
+    g.stage_sort()
+    o.stage_sort()
+    kg, ko = g.read_morton()[:n], o.read_morton()[:n]
+    assert np.all(kg[1:] >= kg[:-1])
+    assert np.array_equal(kg, ko)
+    assert np.array_equal(g.read_index()[:n], o.read_index()[:n])
+
+
+def test_sort_duplicate_keys_stable(gbh_lib, oracle_mod):
+    # many bodies on few lattice points: long runs of equal keys, the order
+    # inside each run must be the compaction order (stable sort)
+    n = 50000
+    rng = np.random.default_rng(5)
+    b = plummer_case(n, seed=5)
+    b["pos_mass"][:, :3] = rng.integers(0, 4, (n, 3)).astype(np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, np.array([0, 0, 0, 3, 3, 3], np.float32))
+    p = abi.step_params(bounds=abi.BOUNDS_STATIC)
+    _prepare_both(g, o, p)
+    g.stage_sort()
+    o.stage_sort()
+    assert np.array_equal(g.read_morton()[:n], o.read_morton()[:n])
+    assert np.array_equal(g.read_index()[:n], o.read_index()[:n])
+
+
+TOPO = ["child_a", "child_b", "bodies_contained", "parent_id", "node_depth", "ready_children"]
+
+
+def _tree_both(g, o, p):
+    _prepare_both(g, o, p)
+    for x in (g, o):
+        x.stage_sort()
+        x.stage_build()
+
+
+@pytest.mark.parametrize("n", [2, 3, 17, 4096, 100000])
+def test_build_topology_bit_exact(gbh_lib, oracle_mod, n):
+    b = plummer_case(n, seed=11 + n)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds_of(b))
+    p = abi.step_params()
+    _tree_both(g, o, p)
+    ig, io = g.read_internal_nodes()[: n - 1], o.read_internal_nodes()[: n - 1]
+    for f in TOPO:
+        assert np.array_equal(ig[f], io[f]), f
+    assert np.array_equal(g.read_leaf_nodes()[:n]["parent_id"], o.read_leaf_nodes()[:n]["parent_id"])
+
+
+def test_build_duplicate_keys(gbh_lib, oracle_mod):
+    n = 20000
+    rng = np.random.default_rng(9)
+    b = plummer_case(n, seed=9)
+    b["pos_mass"][:, :3] = rng.integers(0, 3, (n, 3)).astype(np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, np.array([0, 0, 0, 2, 2, 2], np.float32))
+    p = abi.step_params(bounds=abi.BOUNDS_STATIC)
+    _tree_both(g, o, p)
+    ig, io = g.read_internal_nodes()[: n - 1], o.read_internal_nodes()[: n - 1]
+    for f in TOPO:
+        assert np.array_equal(ig[f], io[f]), f
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4096, 65536])
+def test_fill_bit_exact(gbh_lib, oracle_mod, n):
+    b = plummer_case(n, seed=21 + n)
+    bounds = bounds_of(b) if n > 1 else np.array([-1, -1, -1, 1, 1, 1], np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds)
+    p = abi.step_params()
+    _tree_both(g, o, p)
+    g.stage_fill()
+    o.stage_fill()
+    ni = max(n - 1, 1)
+    ig, io = g.read_internal_nodes()[:ni], o.read_internal_nodes()[:ni]
+    lg, lo = g.read_leaf_nodes()[:n], o.read_leaf_nodes()[:n]
+    for a, c in ((ig, io), (lg, lo)):
+        for f in ("com_mass", "aabb"):
+            assert np.array_equal(a[f].view(np.uint32), c[f].view(np.uint32)), f
+        for f in ("node_depth", "ready_children", "child_a", "child_b", "parent_id", "bodies_contained"):
+            assert np.array_equal(a[f], c[f]), f
+        # star colour uses powf/logf: CUDA and libm may differ in the last ulps
+        np.testing.assert_allclose(a["avg_color"], c["avg_color"], rtol=1e-5, atol=1e-6)
+    assert g.read_stats().tree_height == o.read_stats().tree_height
+
+
+@pytest.mark.parametrize("n,theta", [(4096, 0.5), (65536, 0.5), (65536, 0.3), (30000, 0.7)])
+def test_walk_accel_parity(gbh_lib, oracle_mod, n, theta):
+    b = plummer_case(n, seed=31 + n)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds_of(b))
+    p = abi.step_params(theta=theta, softening=1e-4, flags=abi.FLAG_STORE_ACCEL)
+    for x in (g, o):
+        x.stage_reset(p)
+        x.stage_prepare(p)
+        x.stage_sort()
+        x.stage_build()
+        x.stage_fill()
+        x.stage_walk(p)
+    ag, ao = g.read_accel()[:, :3], o.read_accel()[:, :3]
+    e = rel_err(ag, ao)
+    assert np.median(e) < ACCEL_MEDIAN_TOL, np.median(e)
+    assert np.percentile(e, 99) < 1e-3
+    sg, so = g.read_stats(), o.read_stats()
+    # MAC decisions at the exact boundary may flip with the last ulp of rsqrt
+    assert abs(int(sg.interactions) - int(so.interactions)) <= 1e-4 * so.interactions + 10
+    assert sg.error_word == 0
+
+
+def test_step_graph_equals_stages(gbh_lib, oracle_mod):
+    n = 20000
+    b = plummer_case(n, seed=3)
+    p = abi.step_params(theta=0.5)
+    a = BarnesHut(n, bounds_of(b), abi.units(G=1.0))
+    c = BarnesHut(n, bounds_of(b), abi.units(G=1.0))
+    for x in (a, c):
+        x.upload_bodies(b)
+        x.init()
+    for _ in range(3):
+        a.step(p)
+        c.stage_reset(p)
+        c.stage_prepare(p)
+        c.stage_sort()
+        c.stage_build()
+        c.stage_fill()
+        c.stage_walk(p)
+        c.stage_merge(p)
+        c.stage_swap()
+    a.synchronize()
+    assert np.array_equal(a.read_bodies().view(np.uint32), c.read_bodies().view(np.uint32))
+    assert np.array_equal(a.read_index(), c.read_index())
+    assert np.array_equal(a.read_morton()[:n], c.read_morton()[:n])
+
+
+def test_multi_step_trajectory(gbh_lib, oracle_mod):
+    n = 65536
+    b = plummer_case(n, seed=0)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds_of(b))
+    p = abi.step_params(dt=1e-3, theta=0.5, softening=1e-4)
+    for _ in range(5):
+        g.step(p)
+        o.step(p)
+    pg, po = g.read_bodies()["pos_mass"], o.read_bodies()["pos_mass"]
+    e = np.abs(pg[:, :3] - po[:, :3]).max(axis=1)
+    assert np.median(e) < 1e-6
+    assert np.max(e) < 1e-3
+    sg, so = g.read_sim_values(), o.read_sim_values()
+    assert sg.num_bodies == so.num_bodies == n
+
+
+def test_merge_and_oob_step(gbh_lib, oracle_mod):
+    from gravity_gb300 import ic
+
+    n = 20000
+    b = ic.uniform_merge(n, seed=1)
+    # densify so that merges happen, and push a few bodies out of bounds
+    b["pos_mass"][:, :3] *= 0.25
+    b["pos_mass"][:50, 0] = 3.0
+    bounds = np.array([-2, -2, -2, 2, 2, 2], np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds)
+    p = abi.step_params(dt=5e-4, theta=0.7, softening=1e-4, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+    for x in (g, o):
+        x.stage_reset(p)
+        x.stage_prepare(p)
+        x.stage_sort()
+        x.stage_build()
+        x.stage_fill()
+        x.stage_walk(p)
+    tg, to = g.read_merge_tasks(), o.read_merge_tasks()
+    assert len(to) > 10
+    assert set(map(tuple, tg.tolist())) == set(map(tuple, to.tolist()))
+    g.stage_merge(p)
+    o.stage_merge(p)
+    sg, so = g.read_stats(), o.read_stats()
+    assert sg.merged == so.merged
+    assert sg.out_of_bounds == so.out_of_bounds == 50
+    bg, bo = g.read_bodies(abi.BODIES_OUT), o.read_bodies(abi.BODIES_OUT)
+    assert np.array_equal(bg["pos_mass"][:, 3] == 0, bo["pos_mass"][:, 3] == 0)
+    np.testing.assert_allclose(bg["pos_mass"], bo["pos_mass"], rtol=1e-5, atol=1e-6)
+    # the next step compacts the killed and merged bodies
+    for x in (g, o):
+        x.stage_swap()
+        x.step(p)
+    assert g.read_sim_values().num_bodies == o.read_sim_values().num_bodies
+    assert g.read_sim_values().out_of_bounds == o.read_sim_values().out_of_bounds
+
+
+def test_collision_mode_parity(gbh_lib, oracle_mod):
+    from gravity_gb300 import ic
+
+    n = 8192
+    b = ic.uniform_merge(n, seed=4)
+    b["pos_mass"][:, :3] *= 0.2
+    b["vel_density"][:, :3] = np.random.default_rng(4).normal(0, 0.1, (n, 3))
+    g, o = make_pair(oracle_mod, BarnesHut, b, np.array([-1, -1, -1, 1, 1, 1], np.float32))
+    p = abi.step_params(dt=5e-4, theta=0.7, softening=1e-4, mode=abi.MODE_COLLISION, bounds=abi.BOUNDS_STATIC,
+                        wrap=True, elasticity=0.5)
+    g.step(p)
+    o.step(p)
+    bg, bo = g.read_bodies(), o.read_bodies()
+    np.testing.assert_allclose(bg["pos_mass"], bo["pos_mass"], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(bg["vel_density"], bo["vel_density"], rtol=1e-3, atol=1e-4)
+
+
+def test_direct_sum_matches_fp64(gbh_lib, oracle_mod):
+    n = 30000
+    b = plummer_case(n, seed=2)
+    g = BarnesHut(n, bounds_of(b), abi.units(G=1.0))
+    g.upload_bodies(b)
+    g.init()
+    p = abi.step_params(softening=1e-4)
+    sample = np.arange(0, n, 97, dtype=np.uint32)
+    got = g.direct_sum(p, sample)
+    ref = oracle_mod.direct_sum_fp64(b, sample, 1.0, 1e-4)
+    assert rel_err(got, ref).max() < 1e-5
