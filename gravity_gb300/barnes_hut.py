@@ -111,7 +111,7 @@ class BarnesHut:
     def swap_body_buffers(self):
         self._chk(lib().gbh_stage_swap(self._h))
 
-    # oracle-compatible aliases (the CPU oracle uses the same names)
+    # short names following the C ABI's gbh_stage_* entry points
     stage_reset = reset_values
     stage_prepare = partition_dead_bodies
     stage_sort = radix_sort

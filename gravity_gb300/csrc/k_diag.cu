@@ -40,12 +40,7 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum(const gbh_body* __res
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < DS_TILE; k += DS_THREADS) {
             const uint32_t j = base + k;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (j < j1) {
-                v = ld_pos_mass(bodies, j);
-                if (j == i && valid) v.w = 0.0f;  // self excluded
-            }
-            s_src[k] = v;
+            s_src[k] = j < j1 ? ld_pos_mass(bodies, j) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
         __syncthreads();
         const uint32_t cnt = min((uint32_t)DS_TILE, j1 - base);
@@ -53,7 +48,9 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum(const gbh_body* __res
             const float4 s = s_src[k];
             if (s.w == 0.0f) continue;
             const float rx = s.x - me.x, ry = s.y - me.y, rz = s.z - me.z;
-            const float d2 = rx * rx + ry * ry + rz * rz + soft;
+            const float rr = rx * rx + ry * ry + rz * rz;
+            if (rr == 0.0f) continue;  // the body itself (a zero vector adds nothing)
+            const float d2 = rr + soft;
             const float inv = 1.0f / sqrtf(d2);
             const float f = G * s.w * inv * inv * inv;
             two_sum(hx, lx, f * rx);

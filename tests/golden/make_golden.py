@@ -1,0 +1,111 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference harness.
+
+The harness (oracle/ref_glsl, oracle/ref_harness.py) runs the reference's own
+GLSL compute kernels compiled as C++; it exists only where the reference
+sources are mounted.  Each fixture stores its input bodies, bounds, units and
+step parameters and the reference's outputs, so tests can check the CPU oracle
+and the GPU path against the reference anywhere.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from gravity_gb300 import abi, ic  # noqa: E402
+from oracle import ref_harness as R  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+PARAM_FIELDS = ["dt", "theta", "softening", "elasticity", "restitution", "merging_collision_or_neither",
+                "static_or_dynamic", "wrap_around"]
+
+
+def plummer_with_defects(n, seed):
+    b = ic.plummer(n, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    dead = rng.choice(n, n // 20, replace=False)
+    b["pos_mass"][dead, 3] = 0.0
+    b["pos_mass"][rng.choice(n, 2, replace=False), 0] = np.nan
+    b["pos_mass"][rng.choice(n, 3, replace=False), :3] *= 50.0
+    return b
+
+
+def live_bounds(b):
+    ok = (b["pos_mass"][:, 3] != 0) & np.all(np.isfinite(b["pos_mass"][:, :3]), axis=1)
+    p = b["pos_mass"][ok, :3]
+    return np.concatenate([p.min(0), p.max(0)]).astype(np.float32)
+
+
+def cases():
+    yield "plummer_dynamic", plummer_with_defects(1024, 11), None, abi.step_params(
+        dt=1e-3, theta=0.5, softening=1e-4, bounds=abi.BOUNDS_DYNAMIC), 3
+    b = ic.uniform_merge(1024, seed=12)
+    b["pos_mass"][:, :3] *= 0.05
+    b["pos_mass"][:8, 0] = 3.0
+    yield "merge_static", b, np.array([-2, -2, -2, 2, 2, 2], np.float32), abi.step_params(
+        dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC), 2
+    b = ic.uniform_merge(1024, seed=13)
+    b["pos_mass"][:, :3] *= 0.05
+    b["vel_density"][:, :3] = np.random.default_rng(13).normal(0, 0.1, (1024, 3))
+    yield "collision_wrap", b, np.array([-0.05, -0.05, -0.05, 0.05, 0.05, 0.05], np.float32), abi.step_params(
+        dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_COLLISION, bounds=abi.BOUNDS_STATIC, wrap=True,
+        elasticity=0.5), 2
+    b = ic.plummer(1024, seed=14)
+    b["pos_mass"][:, :3] = np.random.default_rng(14).integers(0, 3, (1024, 3)).astype(np.float32)
+    yield "lattice_duplicates", b, np.array([0, 0, 0, 2, 2, 2], np.float32), abi.step_params(
+        dt=1e-3, theta=0.5, softening=1e-2, bounds=abi.BOUNDS_STATIC), 1
+
+
+def main():
+    units = abi.units(G=1.0)
+    for name, bodies, bounds, p, steps in cases():
+        if bounds is None:
+            bounds = live_bounds(bodies)
+        n = len(bodies)
+        r = R.RefBarnesHut(n, bounds, units)
+        r.upload_bodies(bodies)
+        r.init()
+        per_step = []
+        for _ in range(steps):
+            # stage by stage so the first step's intermediate outputs are kept
+            r.stage_reset(p)
+            r.stage_prepare(p)
+            s = r.read_sim_values()
+            rec = {"prep_index": r.read_index(), "prep_morton": r.read_morton()[: s.num_bodies].copy(),
+                   "prep_bounds": np.array(list(s.bounds_min) + list(s.bounds_max), np.float32),
+                   "prep_num_bodies": s.num_bodies}
+            r.stage_sort()
+            r.stage_build()
+            r.stage_fill()
+            r.stage_walk(p)
+            rec["tasks"] = r.read_merge_tasks()
+            r.stage_merge(p)
+            r.stage_swap()
+            nl = s.num_bodies
+            rec.update({
+                "sorted_index": r.read_index()[:nl].copy(), "sorted_morton": r.read_morton()[:nl].copy(),
+                "internal": r.read_internal_nodes()[: max(nl - 1, 1)].copy(), "leaf": r.read_leaf_nodes()[:nl].copy(),
+                "bodies_after": r.read_bodies(), "uint_debug0": r.read_sim_values().uint_debug[0],
+                "out_of_bounds": r.read_sim_values().out_of_bounds,
+            })
+            per_step.append(rec)
+        r.close()
+        arrays = {"bodies": bodies, "bounds": bounds, "steps": steps,
+                  "params": np.array([float(getattr(p, f)) for f in PARAM_FIELDS])}
+        for k, rec in enumerate(per_step):
+            for key, v in rec.items():
+                arrays[f"s{k}_{key}"] = np.asarray(v)
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, **arrays)
+        print(path, os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    main()

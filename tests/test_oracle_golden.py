@@ -1,0 +1,17 @@
+"""The CPU oracle against golden vectors produced by the reference's own GLSL
+kernels (tests/golden, generated by tests/golden/make_golden.py): every stage
+output and the bodies after each step must be bit-identical."""
+import os
+
+import pytest
+
+from .golden_check import fixtures, replay
+
+
+@pytest.mark.parametrize("path", fixtures(), ids=lambda p: os.path.basename(p))
+def test_oracle_matches_reference_golden(oracle_mod, path):
+    assert replay(path, oracle_mod.OracleBarnesHut, exact_walk=True, ordered_tasks=True)
+
+
+def test_golden_fixtures_present():
+    assert len(fixtures()) >= 4
