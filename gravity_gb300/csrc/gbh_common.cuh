@@ -29,12 +29,19 @@
 #define PREP_TILE (PREP_THREADS * PREP_ITEMS)
 
 // Compact node record read by the walk: 32 bytes = one DRAM sector.
-struct __align__(16) WalkNode {
-    float4 cm;        // centre of mass xyz, mass
-    float half_side;  // getLongestSide(node), bh_force.comp:14-20
-    uint32_t child_a;
-    uint32_t child_b;
+struct __align__(16) WalkRec {
+    float4 cm;        // centre of mass xyz, mass (a leaf: the body's posMass)
+    float half_side;  // getLongestSide(node), bh_force.comp:14-20 (0 for a leaf)
+    uint32_t id;      // global node id: < N leaf (sorted slot), >= N internal
     uint32_t count;   // bodies contained
+    uint32_t pad;
+};
+
+// The records of both children of one internal node, written by the fill and
+// read by the walk with one 64-byte load when the node is opened.
+struct __align__(16) ChildPair {
+    WalkRec a;  // childA
+    WalkRec b;  // childB
 };
 
 // Device-resident state of one step (never read by the reference-facing
@@ -75,7 +82,8 @@ struct StepBuffers {
     uint32_t* idx_out;
     gbh_node* leaf;
     gbh_node* internal;
-    WalkNode* wnode;
+    ChildPair* pairs;     // per internal node
+    WalkRec* root_rec;    // record of the root (internal node 0)
     float4* leaf_pm;      // sorted-order copy of posMass (leaf comMass)
     float* leaf_rad;      // sorted-order radius(body)
     gbh_sim_values* sim;
@@ -153,6 +161,14 @@ __device__ __forceinline__ void st_body(gbh_body* b, uint32_t i, float4 pm, floa
     float4* p = reinterpret_cast<float4*>(b) + 2 * (size_t)i;
     p[0] = pm;
     p[1] = vd;
+}
+
+// device-scope acquire-release atomic add (orders this thread's earlier writes
+// before the add and the sibling's released writes before later reads)
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }

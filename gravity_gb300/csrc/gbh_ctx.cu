@@ -60,7 +60,8 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.idx_out = c->idx[1 - c->iin];
     b.leaf = c->leaf;
     b.internal = c->internal;
-    b.wnode = c->wnode;
+    b.pairs = c->pairs;
+    b.root_rec = c->root_rec;
     b.leaf_pm = c->leaf_pm;
     b.leaf_rad = c->leaf_rad;
     b.sim = c->sim;
@@ -203,7 +204,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_keys0 = A.add((size_t)n * 8), o_keys1 = A.add((size_t)n * 8);
     size_t o_idx0 = A.add((size_t)n * 4), o_idx1 = A.add((size_t)n * 4);
     size_t o_leaf = A.add((size_t)n * 80), o_int = A.add((size_t)ni * 80);
-    size_t o_wnode = A.add((size_t)ni * sizeof(WalkNode));
+    size_t o_pairs = A.add((size_t)ni * sizeof(ChildPair)), o_root = A.add(sizeof(WalkRec));
     size_t o_lpm = A.add((size_t)n * 16), o_lrad = A.add((size_t)n * 4);
     size_t o_sim = A.add(sizeof(gbh_sim_values)), o_st = A.add(sizeof(DevState));
     size_t o_par = A.add(sizeof(gbh_step_params));
@@ -229,7 +230,8 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->idx[1] = (uint32_t*)(base + o_idx1);
     c->leaf = (gbh_node*)(base + o_leaf);
     c->internal = (gbh_node*)(base + o_int);
-    c->wnode = (WalkNode*)(base + o_wnode);
+    c->pairs = (ChildPair*)(base + o_pairs);
+    c->root_rec = (WalkRec*)(base + o_root);
     c->leaf_pm = (float4*)(base + o_lpm);
     c->leaf_rad = (float*)(base + o_lrad);
     c->sim = (gbh_sim_values*)(base + o_sim);

@@ -27,7 +27,8 @@ struct gbh_ctx {
     int iin = 0;  // keys[iin], idx[iin] are MortonIn / IndexIn
     gbh_node* leaf = nullptr;
     gbh_node* internal = nullptr;
-    WalkNode* wnode = nullptr;
+    ChildPair* pairs = nullptr;
+    WalkRec* root_rec = nullptr;
     float4* leaf_pm = nullptr;
     float* leaf_rad = nullptr;
     gbh_sim_values* sim = nullptr;

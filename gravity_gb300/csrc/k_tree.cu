@@ -120,14 +120,14 @@ struct NodeVals {
     uint32_t depth;
 };
 
-// L2-coherent read of a node written by another thread of this kernel
+// L2-coherent read of the fields of a node written by another thread of this kernel
 __device__ __forceinline__ NodeVals load_node_cg(const gbh_node* nd) {
     NodeVals v;
     const float4* p = reinterpret_cast<const float4*>(nd);
     v.cm = __ldcg(p + 0);
     const float4 a = __ldcg(p + 1);
-    const float4 c = __ldcg(p + 2);  // aabb4, aabb5, childA, childB
-    const uint4 e = __ldcg(reinterpret_cast<const uint4*>(p + 3));
+    const float2 c = __ldcg(reinterpret_cast<const float2*>(p + 2));  // aabb4, aabb5
+    v.depth = __ldcg(reinterpret_cast<const uint32_t*>(p + 3));
     v.col = __ldcg(p + 4);
     v.box[0] = a.x;
     v.box[1] = a.y;
@@ -135,8 +135,22 @@ __device__ __forceinline__ NodeVals load_node_cg(const gbh_node* nd) {
     v.box[3] = a.w;
     v.box[4] = c.x;
     v.box[5] = c.y;
-    v.depth = e.x;
     return v;
+}
+
+__device__ __forceinline__ float half_side(const float box[6]) {
+    const float ex = box[3] - box[0], ey = box[4] - box[1], ez = box[5] - box[2];
+    return gmax(ex, gmax(ey, ez)) / 2.0f;
+}
+
+__device__ __forceinline__ WalkRec make_rec(const NodeVals& v, uint32_t id, uint32_t count, bool leaf) {
+    WalkRec r;
+    r.cm = v.cm;
+    r.half_side = leaf ? 0.0f : half_side(v.box);
+    r.id = id;
+    r.count = count;
+    r.pad = 0;
+    return r;
 }
 
 __global__ __launch_bounds__(256) void k_fill(StepBuffers b) {
@@ -152,88 +166,104 @@ __global__ __launch_bounds__(256) void k_fill(StepBuffers b) {
     gbh_node* lf = &b.leaf[g];
     float4* lp = reinterpret_cast<float4*>(lf);
     const uint32_t parent0 = lf->parent_id;
+    NodeVals own;
+    own.cm = pm;
+    own.box[0] = own.box[3] = pm.x;
+    own.box[1] = own.box[4] = pm.y;
+    own.box[2] = own.box[5] = pm.z;
+    own.col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    own.depth = 0;
+    if (pm.w > 0.0f && vd.w > 0.0f) {
+        float rgb[3];
+        star_color(pm.w * sim->unit_mass, vd.w * sim->unit_density, rgb);
+        own.col = make_float4(rgb[0], rgb[1], rgb[2], 0.0f);
+    }
     lp[0] = pm;
     lp[1] = make_float4(pm.x, pm.y, pm.z, pm.x);
     reinterpret_cast<uint4*>(lp)[2] = make_uint4(__float_as_uint(pm.y), __float_as_uint(pm.z), GBH_NONE, GBH_NONE);
     reinterpret_cast<uint4*>(lp)[3] = make_uint4(0u, 0u, GBH_NONE, parent0);
-    float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (pm.w > 0.0f && vd.w > 0.0f) {
-        float rgb[3];
-        star_color(pm.w * sim->unit_mass, vd.w * sim->unit_density, rgb);
-        col = make_float4(rgb[0], rgb[1], rgb[2], 0.0f);
-    }
-    lp[4] = col;
+    lp[4] = own.col;
     b.leaf_pm[g] = pm;
     if (b.params->merging_collision_or_neither != GBH_MODE_NEITHER)
         b.leaf_rad[g] = body_radius(sim->body_length_constant, pm.w, vd.w);
 
-    // climb
+    // climb: the second child to arrive at a node finishes it
+    uint32_t self = g;          // global id of the node whose values are in `own`
+    uint32_t self_count = 1;
     uint32_t node = parent0;
     while (node != GBH_NONE) {
         const uint32_t i = node - N;
         gbh_node* nd = &b.internal[i];
-        __threadfence();
-        const uint32_t old = atomicAdd(&nd->ready_children, 1u);
-        if (old == 0u) return;  // first child to arrive; the sibling finishes this node
-        __threadfence();
-        const uint32_t ca = nd->child_a, cb = nd->child_b;
-        NodeVals L = load_node_cg(ca < N ? &b.leaf[ca] : &b.internal[ca - N]);
-        NodeVals R;
-        if (cb == GBH_NONE) {  // single-body tree: the missing child contributes nothing
-            R.cm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            R.col = R.cm;
-            R.box[0] = R.box[1] = R.box[2] = 1e38f;
-            R.box[3] = R.box[4] = R.box[5] = -1e38f;
-            R.depth = 0;
+        // release: own node's writes before the count; acquire: the sibling's writes after it
+        const uint32_t old = atomic_add_acq_rel(&nd->ready_children, 1u);
+        if (old == 0u) return;
+        const uint2 kids = *reinterpret_cast<const uint2*>(&nd->child_a);
+        const bool self_is_a = kids.x == self;
+        const uint32_t sib = self_is_a ? kids.y : kids.x;
+        NodeVals S;
+        uint32_t sib_count = 1;
+        if (sib == GBH_NONE) {  // single-body tree: the missing child contributes nothing
+            S.cm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            S.col = S.cm;
+            S.box[0] = S.box[1] = S.box[2] = 1e38f;
+            S.box[3] = S.box[4] = S.box[5] = -1e38f;
+            S.depth = 0;
+            sib_count = 0;
+        } else if (sib < N) {
+            S = load_node_cg(&b.leaf[sib]);
         } else {
-            R = load_node_cg(cb < N ? &b.leaf[cb] : &b.internal[cb - N]);
+            S = load_node_cg(&b.internal[sib - N]);
+            sib_count = __ldcg(&b.internal[sib - N].bodies_contained);
         }
+        const NodeVals& L = self_is_a ? own : S;
+        const NodeVals& R = self_is_a ? S : own;
         // bh_tree.comp:223-246
         const float lw = L.cm.w, rw = R.cm.w;
         const float M = lw + rw;
-        float c[3], a[3];
-        const float lc[3] = {L.cm.x, L.cm.y, L.cm.z}, rc[3] = {R.cm.x, R.cm.y, R.cm.z};
-        const float la[3] = {L.col.x, L.col.y, L.col.z}, ra[3] = {R.col.x, R.col.y, R.col.z};
+        NodeVals out;
         if (M > 0.0f) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                c[k] = (lw * lc[k] + rw * rc[k]) / M;
-                a[k] = (lw * la[k] + rw * ra[k]) / M;
-            }
+            out.cm.x = (lw * L.cm.x + rw * R.cm.x) / M;
+            out.cm.y = (lw * L.cm.y + rw * R.cm.y) / M;
+            out.cm.z = (lw * L.cm.z + rw * R.cm.z) / M;
+            out.col.x = (lw * L.col.x + rw * R.col.x) / M;
+            out.col.y = (lw * L.col.y + rw * R.col.y) / M;
+            out.col.z = (lw * L.col.z + rw * R.col.z) / M;
         } else {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                c[k] = (lc[k] + rc[k]) * 0.5f;
-                a[k] = (la[k] + ra[k]) * 0.5f;
-            }
+            out.cm.x = (L.cm.x + R.cm.x) * 0.5f;
+            out.cm.y = (L.cm.y + R.cm.y) * 0.5f;
+            out.cm.z = (L.cm.z + R.cm.z) * 0.5f;
+            out.col.x = (L.col.x + R.col.x) * 0.5f;
+            out.col.y = (L.col.y + R.col.y) * 0.5f;
+            out.col.z = (L.col.z + R.col.z) * 0.5f;
         }
-        float box[6];
+        out.cm.w = M;
+        out.col.w = 0.0f;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            box[k] = gmin(L.box[k], R.box[k]);
-            box[3 + k] = gmax(L.box[3 + k], R.box[3 + k]);
+            out.box[k] = gmin(L.box[k], R.box[k]);
+            out.box[3 + k] = gmax(L.box[3 + k], R.box[3 + k]);
         }
-        const uint32_t depth = 1u + max(L.depth, R.depth);
+        out.depth = 1u + max(L.depth, R.depth);
         float4* np = reinterpret_cast<float4*>(nd);
-        __stcg(np + 0, make_float4(c[0], c[1], c[2], M));
-        __stcg(np + 1, make_float4(box[0], box[1], box[2], box[3]));
-        __stcg(reinterpret_cast<float2*>(np + 2), make_float2(box[4], box[5]));
-        nd->node_depth = depth;
+        __stcg(np + 0, out.cm);
+        __stcg(np + 1, make_float4(out.box[0], out.box[1], out.box[2], out.box[3]));
+        __stcg(reinterpret_cast<float2*>(np + 2), make_float2(out.box[4], out.box[5]));
+        nd->node_depth = out.depth;
         nd->ready_children = GBH_NONE;
-        __stcg(np + 4, make_float4(a[0], a[1], a[2], 0.0f));
-        // walk record, getLongestSide: bh_force.comp:14-20
-        const float ex = box[3] - box[0], ey = box[4] - box[1], ez = box[5] - box[2];
-        const float half = gmax(ex, gmax(ey, ez)) / 2.0f;
-        WalkNode wn;
-        wn.cm = make_float4(c[0], c[1], c[2], M);
-        wn.half_side = half;
-        wn.child_a = ca;
-        wn.child_b = cb;
-        wn.count = nd->bodies_contained;
-        b.wnode[i] = wn;
+        __stcg(np + 4, out.col);
+        // walk records of both children
+        ChildPair pr;
+        const uint32_t a_id = self_is_a ? self : sib, b_id = self_is_a ? sib : self;
+        pr.a = make_rec(L, a_id, self_is_a ? self_count : sib_count, a_id < N);
+        pr.b = make_rec(R, b_id, self_is_a ? sib_count : self_count, b_id < N);
+        b.pairs[i] = pr;
+        self = node;
+        self_count = self_count + sib_count;
+        own = out;
         const uint32_t parent = nd->parent_id;
         if (parent == GBH_NONE) {
-            b.st->tree_height = depth;
+            b.st->tree_height = out.depth;
+            *b.root_rec = make_rec(out, node, self_count, false);
             return;
         }
         node = parent;

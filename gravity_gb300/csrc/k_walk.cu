@@ -6,22 +6,39 @@
 // visit and a global atomic per opened node.
 //
 // Here a warp walks for 32 consecutive bodies of the Morton order (spatial
-// neighbours) with ONE shared stack in shared memory.  Each stack entry
-// carries the mask of lanes that opened its parent; a lane evaluates only the
-// entries that carry its bit, so every lane visits exactly the nodes its own
-// reference walk would visit, in the same depth-first order (childB popped
-// before childA), and accumulates the same terms in the same order.  Node
-// records are 32-byte WalkNodes (one sector) read warp-uniformly, so a visit
-// is one broadcast load instead of 32 divergent 80-byte gathers.  The per-node
-// debug atomic of the reference (bh_force.comp:72) becomes one add per warp.
+// neighbours) with ONE shared stack.  Each stack entry carries the mask of
+// lanes that opened its parent; a lane evaluates only the entries that carry
+// its bit, so every lane visits exactly the nodes its own reference walk would
+// visit, in the same depth-first order (childB evaluated before childA), and
+// accumulates its terms in that order.
+//
+// Node data travel with the traversal: opening a node reads its ChildPair
+// (the 32-byte records of both children, one 64-byte warp-uniform load);
+// childB is evaluated next straight from registers and childA is pushed, with
+// its record, on the warp's shared-memory stack.  A visit therefore costs no
+// global load of its own, and one load serves two visits.  The per-node debug
+// atomic of the reference (bh_force.comp:72) becomes one add per warp.
+//
+// Arithmetic: the MAC is the reference's (half side * invDist < theta, with
+// invDist from the softened distance); the force sum uses fused multiply-adds
+// (G m inv^3 r accumulated with FMA), which is within 1e-7 relative of the
+// reference's operation order.
 #include "gbh_common.cuh"
 
 #define WALK_THREADS 256
 #define WALK_WARPS (WALK_THREADS / 32)
+#define WALK_STACK 128
+
+struct __align__(16) StackEntry {
+    float4 cm;
+    float half;
+    uint32_t id;
+    uint32_t mask;
+    uint32_t pad;
+};
 
 __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
-    __shared__ uint32_t s_node[WALK_WARPS][GBH_WALK_STACK];
-    __shared__ uint32_t s_mask[WALK_WARPS][GBH_WALK_STACK];
+    __shared__ StackEntry s_stack[WALK_WARPS][WALK_STACK];
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
@@ -34,115 +51,118 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     const float G = sim->gravitational_constant;
     const float soft = P->softening, theta = P->theta;
     const uint32_t mode = P->merging_collision_or_neither;
-    const float4* __restrict__ leaf_pm = b.leaf_pm;
-    const WalkNode* __restrict__ wn = b.wnode;
+    const ChildPair* __restrict__ pairs = b.pairs;
+    StackEntry* stk = s_stack[w];
 
     const uint32_t bi = active ? b.idx_in[g] : 0u;
-    float4 pm = active ? leaf_pm[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 pm = active ? b.leaf_pm[g] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 vd = active ? ld_vel_density(b.bodies_in, bi) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float my_rad = (active && mode != GBH_MODE_NEITHER) ? b.leaf_rad[g] : 0.0f;
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     uint32_t inter = 0, seq = 0;
-    uint32_t opened = 0;  // lane 0 only
-    uint32_t max_sp = 0;
+    uint32_t opened = 0;
+    uint32_t sp = 0, max_sp = 0;
     bool overflow = false;
 
-    int sp = 0;
-    const uint32_t act_mask = __ballot_sync(0xffffffffu, active);
-    if (n > 1) {
-        if (lane == 0) {
-            s_node[w][0] = N;  // root, bh_force.comp:53
-            s_mask[w][0] = act_mask;
-        }
-        sp = 1;
+    // current entry (warp-uniform): starts at the root, bh_force.comp:53
+    float4 cur_cm;
+    float cur_half;
+    uint32_t cur_id, cur_mask;
+    {
+        const WalkRec root = *b.root_rec;
+        cur_cm = root.cm;
+        cur_half = root.half_side;
+        cur_id = N;
+        cur_mask = __ballot_sync(0xffffffffu, active);
     }
-    __syncwarp();
-    while (sp > 0) {
-        --sp;
-        const uint32_t node = s_node[w][sp];
-        const uint32_t mask = s_mask[w][sp];
-        __syncwarp();
-        const bool me = (mask >> lane) & 1u;
-        if (node >= N) {
-            const WalkNode* p = wn + (node - N);
-            const float4 cm = __ldg(&p->cm);
-            const uint4 rest = __ldg(reinterpret_cast<const uint4*>(p) + 1);
-            const float half = __uint_as_float(rest.x);
-            const float rx = cm.x - pm.x, ry = cm.y - pm.y, rz = cm.z - pm.z;
-            const float d2 = rx * rx + ry * ry + rz * rz + soft;
-            const float inv = rsqrtf(d2);
-            const bool accept = half * inv < theta;
-            if (me && accept) {
-                const float s = G * cm.w;
-                ax = ax + s * rx * inv * inv * inv;
-                ay = ay + s * ry * inv * inv * inv;
-                az = az + s * rz * inv * inv * inv;
-                ++inter;
-            }
-            const uint32_t om = __ballot_sync(0xffffffffu, me && !accept);
-            if (om) {
-                if (sp + 2 > GBH_WALK_STACK) {
-                    overflow = true;
-                    break;
-                }
-                if (lane == 0) {
-                    s_node[w][sp] = rest.y;      // childA
-                    s_mask[w][sp] = om;
-                    s_node[w][sp + 1] = rest.z;  // childB, popped first
-                    s_mask[w][sp + 1] = om;
-                    opened += __popc(om);
-                }
-                sp += 2;
-                max_sp = max(max_sp, (uint32_t)sp);
-                __syncwarp();
-            }
+    const bool walk = n > 1;
+    while (walk) {
+        const bool me = (cur_mask >> lane) & 1u;
+        const float rx = cur_cm.x - pm.x, ry = cur_cm.y - pm.y, rz = cur_cm.z - pm.z;
+        const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
+        const float inv = rsqrtf(rr + soft);
+        bool open = false, interact;
+        if (cur_id >= N) {
+            const bool accept = cur_half * inv < theta;
+            interact = me && accept;
+            open = me && !accept;
         } else {
-            // leaf: sorted slot `node`; skip the body's own leaf (bh_force.comp:76-78)
-            const float4 o = __ldg(leaf_pm + node);
-            if (me && node != g) {
-                const float rx = o.x - pm.x, ry = o.y - pm.y, rz = o.z - pm.z;
-                const float rr = rx * rx + ry * ry + rz * rz;
-                const float inv = rsqrtf(rr + soft);
-                const float s = G * o.w;
-                ax = ax + s * rx * inv * inv * inv;
-                ay = ay + s * ry * inv * inv * inv;
-                az = az + s * rz * inv * inv * inv;
-                ++inter;
-                if (mode != GBH_MODE_NEITHER) {
-                    const uint32_t oi = b.idx_in[node];
-                    const float orad = b.leaf_rad[node];
-                    const float dist = sqrtf(rr);
-                    const float pen = my_rad + orad - dist;
-                    if (mode == GBH_MODE_COLLISION && pen > 0.0f) {
-                        // bh_force.comp:93-107
-                        const float4 ov = ld_vel_density(b.bodies_in, oi);
-                        const float vx = ov.x - vd.x, vy = ov.y - vd.y, vz = ov.z - vd.z;
-                        const float len = sqrtf(rr);
-                        const float nx = rx / len, ny = ry / len, nz = rz / len;
-                        const float vimp = vx * nx + vy * ny + vz * nz;
-                        if (vimp < 0.0f) {
-                            const float meff = 1.0f / (1.0f / pm.w + 1.0f / o.w);
-                            const float imp = (1.0f + P->elasticity) * meff * vimp;
-                            vd.x += nx * imp / pm.w;
-                            vd.y += ny * imp / pm.w;
-                            vd.z += nz * imp / pm.w;
-                        }
-                        const float sc = pen / (pm.w + o.w) * P->restitution;
-                        pm.x -= sc * nx;
-                        pm.y -= sc * ny;
-                        pm.z -= sc * nz;
+            interact = me && cur_id != g;  // the body's own leaf, bh_force.comp:76-78
+        }
+        if (interact) {
+            const float f = G * cur_cm.w * (inv * inv * inv);
+            ax = __fmaf_rn(f, rx, ax);
+            ay = __fmaf_rn(f, ry, ay);
+            az = __fmaf_rn(f, rz, az);
+            ++inter;
+            if (mode != GBH_MODE_NEITHER && cur_id < N) {
+                const uint32_t oi = b.idx_in[cur_id];
+                const float orad = b.leaf_rad[cur_id];
+                const float dist = sqrtf(rx * rx + ry * ry + rz * rz);
+                const float pen = my_rad + orad - dist;
+                if (mode == GBH_MODE_COLLISION && pen > 0.0f) {
+                    // bh_force.comp:93-107, in the reference's operation order
+                    const float ow = cur_cm.w;
+                    const float4 ov = ld_vel_density(b.bodies_in, oi);
+                    const float vx = ov.x - vd.x, vy = ov.y - vd.y, vz = ov.z - vd.z;
+                    const float nx = rx / dist, ny = ry / dist, nz = rz / dist;
+                    const float vimp = vx * nx + vy * ny + vz * nz;
+                    if (vimp < 0.0f) {
+                        const float meff = 1.0f / (1.0f / pm.w + 1.0f / ow);
+                        const float imp = (1.0f + P->elasticity) * meff * vimp;
+                        vd.x += nx * imp / pm.w;
+                        vd.y += ny * imp / pm.w;
+                        vd.z += nz * imp / pm.w;
                     }
-                    if (mode == GBH_MODE_MERGE && pen > 0.0f && bi < oi) {
-                        // bh_force.comp:109-112, plus an ordering key for merge resolution
-                        const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
-                        if (slot < N) {
-                            b.mq->pairs[slot] = make_uint2(bi, oi);
-                            b.mkeys[slot] = ((unsigned long long)g << 32) | seq;
-                        }
-                        ++seq;
+                    const float sc = pen / (pm.w + ow) * P->restitution;
+                    pm.x -= sc * nx;
+                    pm.y -= sc * ny;
+                    pm.z -= sc * nz;
+                }
+                if (mode == GBH_MODE_MERGE && pen > 0.0f && bi < oi) {
+                    // bh_force.comp:109-112, plus an ordering key for merge resolution
+                    const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
+                    if (slot < N) {
+                        b.mq->pairs[slot] = make_uint2(bi, oi);
+                        b.mkeys[slot] = ((unsigned long long)g << 32) | seq;
                     }
+                    ++seq;
                 }
             }
+        }
+        const uint32_t om = __ballot_sync(0xffffffffu, open);
+        if (om) {
+            opened += __popc(om);
+            const float4* q = reinterpret_cast<const float4*>(pairs + (cur_id - N));
+            const float4 a_cm = __ldg(q + 0);
+            const uint4 a_meta = __ldg(reinterpret_cast<const uint4*>(q + 1));
+            const float4 b_cm = __ldg(q + 2);
+            const uint4 b_meta = __ldg(reinterpret_cast<const uint4*>(q + 3));
+            if (sp >= WALK_STACK) {
+                overflow = true;
+                break;
+            }
+            if (lane == 0) {
+                stk[sp].cm = a_cm;
+                *reinterpret_cast<uint4*>(&stk[sp].half) = make_uint4(a_meta.x, a_meta.y, om, 0u);
+            }
+            ++sp;
+            max_sp = max(max_sp, sp);
+            cur_cm = b_cm;
+            cur_half = __uint_as_float(b_meta.x);
+            cur_id = b_meta.y;
+            cur_mask = om;
+        } else {
+            if (sp == 0) break;
+            --sp;
+            __syncwarp();
+            const float4 e_cm = stk[sp].cm;
+            const uint4 e_meta = *reinterpret_cast<const uint4*>(&stk[sp].half);
+            __syncwarp();
+            cur_cm = e_cm;
+            cur_half = __uint_as_float(e_meta.x);
+            cur_id = e_meta.y;
+            cur_mask = e_meta.z;
         }
     }
     if (overflow && lane == 0) set_error(b.st, GBH_DEVERR_WALK_STACK);
@@ -155,7 +175,7 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
         atomicAdd(&b.st->interactions, (unsigned long long)tot);
         atomicAdd(&b.st->opened, (unsigned long long)opened);
         atomicAdd(&b.sim->uint_debug[0], opened);
-        atomicMax(&b.st->max_stack, max_sp);
+        atomicMax(&b.st->max_stack, max_sp + 1);
     }
     if (!active) return;
     if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
