@@ -64,6 +64,7 @@ def _declare(L):
         "gbh_mac_train": [vp, u32, u32, C.c_float, u64, vp],
         "gbh_mac_loss_grad": [vp, vp, vp, u32, C.POINTER(C.c_float), vp],
         "gbh_mac_predict": [vp, vp, u32, vp],
+        "gbh_sort_pairs_noalloc": [vp, vp, vp, vp, u32, vp],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

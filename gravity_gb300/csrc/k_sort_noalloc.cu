@@ -1,0 +1,127 @@
+// k_sort_noalloc.cu — gbh_sort_pairs_noalloc: the step's radix sort for
+// callers that must not allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc is not allowed or not wanted:
+// a host whose device memory is owned by another allocator (a Java or game
+// engine renderer that hands out only its own buffers), code that runs while
+// another component holds the device's memory pool, or a hot loop that must
+// never hit the allocator's locks or device synchronisation.  It sorts
+// (uint64 key, uint32 value) pairs that the caller already has on the device.
+//
+// Scratch: everything the onesweep sort needs beyond the caller's inputs and
+// outputs (a ping-pong copy of the pairs, the digit histograms, the look-back
+// words, the tile tickets and the error word) lives in one file-scope
+// __device__ array below.  Every GPU that loads this library holds it, about
+// 15 MB, until the process exits.  All calls share it: a call clears what must
+// start at zero, and calls that overlap on the GPU (on different streams or
+// threads) race on it; serialise them.
+//
+// The device address of the array is taken once per device, with that device
+// current, by the first call on that device (cudaGetSymbolAddress).  Make
+// that first call before any stream capture.
+#include <mutex>
+
+#include "gbh_common.cuh"
+
+void sort_setup();  // k_sort.cu
+
+#define NOALLOC_MAX_PAIRS (1u << 20)
+#define NOALLOC_TILES ((NOALLOC_MAX_PAIRS + SORT_TILE - 1) / SORT_TILE)
+#define NOALLOC_MAX_DEVICES 64
+
+struct NoAllocScratch {
+    unsigned long long keys_tmp[NOALLOC_MAX_PAIRS];
+    uint32_t vals_tmp[NOALLOC_MAX_PAIRS];
+    uint32_t hist[SORT_PASSES * SORT_RADIX];
+    uint32_t bucket_base[SORT_PASSES * SORT_RADIX];
+    uint32_t lookback[SORT_PASSES * NOALLOC_TILES * SORT_RADIX];
+    DevState st;
+};
+
+static __device__ __align__(256) NoAllocScratch g_sort_scratch;
+
+static NoAllocScratch* g_scratch_ptr[NOALLOC_MAX_DEVICES];
+static std::mutex g_scratch_mu;
+
+// digit histograms of all 8 passes and the live count, into the scratch
+__global__ void k_noalloc_hist(const uint64_t* __restrict__ keys, uint32_t n, NoAllocScratch* s) {
+    __shared__ uint32_t h[SORT_PASSES * SORT_RADIX];
+    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x) h[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) s->st.n_new = n;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < SORT_PASSES; ++p) atomicAdd(&h[p * SORT_RADIX + ((k >> (8 * p)) & 0xFF)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x)
+        if (h[i]) atomicAdd(&s->hist[i], h[i]);
+}
+
+static NoAllocScratch* scratch_for_current_device(int* status) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        *status = GBH_ERR_CUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_sort_scratch) != cudaSuccess || !p) {
+            *status = GBH_ERR_CUDA;
+            return nullptr;
+        }
+        g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
+    }
+    *status = GBH_OK;
+    return g_scratch_ptr[dev];
+}
+
+extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                                      uint32_t* vals_out, uint32_t n, void* stream) {
+    if (n > NOALLOC_MAX_PAIRS) return GBH_ERR_INVALID;
+    if (n == 0) return GBH_OK;
+    if (!keys_in || !vals_in || !keys_out || !vals_out) return GBH_ERR_INVALID;
+    int status = GBH_OK;
+    NoAllocScratch* s = scratch_for_current_device(&status);
+    if (!s) return status;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the sort runs in place in the caller's output buffers
+    if (keys_out != keys_in &&
+        cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return GBH_ERR_CUDA;
+    if (vals_out != vals_in &&
+        cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return GBH_ERR_CUDA;
+    // clear what the previous call left: histograms, tickets, error word, look-back words
+    if (cudaMemsetAsync(s->hist, 0, sizeof(s->hist), st) != cudaSuccess) return GBH_ERR_CUDA;
+    if (cudaMemsetAsync(&s->st, 0, sizeof(s->st), st) != cudaSuccess) return GBH_ERR_CUDA;
+    const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    for (uint32_t p = 0; p < SORT_PASSES; ++p)
+        if (cudaMemsetAsync(s->lookback + (size_t)p * NOALLOC_TILES * SORT_RADIX, 0, (size_t)tiles * SORT_RADIX * 4,
+                            st) != cudaSuccess)
+            return GBH_ERR_CUDA;
+    const uint32_t hblocks = min((n + 255) / 256, 152u * 4u);
+    k_noalloc_hist<<<hblocks, 256, 0, st>>>(keys_out, n, s);
+    StepBuffers b;
+    memset(&b, 0, sizeof(b));
+    b.keys_in = keys_out;
+    b.idx_in = vals_out;
+    b.keys_out = reinterpret_cast<uint64_t*>(s->keys_tmp);
+    b.idx_out = s->vals_tmp;
+    b.st = &s->st;
+    b.hist = s->hist;
+    b.bucket_base = s->bucket_base;
+    b.lookback = s->lookback;
+    b.N = n;
+    b.sort_tiles_cap = NOALLOC_TILES;
+    sort_setup();
+    launch_sort(b, st);
+    if (cudaGetLastError() != cudaSuccess) return GBH_ERR_CUDA;
+    // report errors raised on the device (bounded look-back waits)
+    uint32_t err = 0;
+    if (cudaMemcpyAsync(&err, &s->st.error_word, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return GBH_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return GBH_ERR_CUDA;
+    return err ? GBH_ERR_DEVICE : GBH_OK;
+}

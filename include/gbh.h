@@ -302,6 +302,30 @@ int gbh_mac_loss_grad(gbh_ctx* ctx, const float* features, const float* labels, 
 /* Inference on host features: out[count] predicted log10 error. */
 int gbh_mac_predict(gbh_ctx* ctx, const float* features, uint32_t count, float* out);
 
+/* ---- sorting without allocation ---------------------------------------------
+ * No counterpart in the reference: this entry point is new in this library.
+ * For callers that cannot call cudaMalloc — a host whose device memory belongs
+ * to another allocator or engine, code running while another component owns
+ * the memory pool, or a loop that must never take the allocator's locks or
+ * synchronise the device.  Stable ascending sort of n (uint64 key, uint32
+ * value) pairs by key, on device memory the caller provides (inputs and
+ * outputs may alias; the inputs are left untouched when they do not).  The
+ * same onesweep kernels as the step's sort.
+ *   - n is at most 1,048,576 (GBH_SORT_NOALLOC_MAX_PAIRS); larger n returns
+ *     GBH_ERR_INVALID.
+ *   - Allocates nothing: its scratch (about 15 MB) is a static device array
+ *     that every GPU loading this library holds until exit, shared by all
+ *     calls.  Each call clears what must start at zero; calls that overlap on
+ *     the GPU race on the scratch and must be serialised by the caller.
+ *   - The first call on a device looks up the scratch's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - Runs on `stream` (a cudaStream_t, NULL = default stream) on the current
+ *     device and returns after the sort has finished; GBH_ERR_DEVICE when a
+ *     bounded wait of the sort gave up. */
+#define GBH_SORT_NOALLOC_MAX_PAIRS (1u << 20)
+int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                           uint32_t* vals_out, uint32_t n, void* stream);
+
 /* ---- library info ---------------------------------------------------------- */
 int gbh_abi_version(void);
 const char* gbh_last_error(gbh_ctx* ctx);
