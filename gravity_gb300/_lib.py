@@ -61,6 +61,7 @@ def _declare(L):
         "gbh_mac_generate": [vp, sp, u32, u64, C.POINTER(u32)],
         "gbh_mac_read_pairs": [vp, vp, vp, u32, u32],
         "gbh_mac_write_pairs": [vp, vp, vp, u32],
+        "gbh_mac_read_pair_ids": [vp, vp, u32, u32],
         "gbh_mac_train": [vp, u32, u32, C.c_float, u64, vp],
         "gbh_mac_loss_grad": [vp, vp, vp, u32, C.POINTER(C.c_float), vp],
         "gbh_mac_predict": [vp, vp, u32, vp],

@@ -140,7 +140,7 @@ class Stats(C.Structure):
         ("tree_height", C.c_uint32),
         ("max_stack", C.c_uint32),
         ("error_word", C.c_uint32),
-        ("pad", C.c_uint32),
+        ("frontier_saturated", C.c_uint32),
     ]
 
 

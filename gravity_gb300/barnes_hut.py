@@ -204,3 +204,68 @@ class BarnesHut:
         out = np.zeros((len(s), 3), dtype=np.float64)
         self._chk(lib().gbh_direct_sum(self._h, C.byref(params), _ptr(s), len(s), _ptr(out)))
         return out
+
+    def evaluate_walk(self, params: abi.StepParams) -> np.ndarray:
+        """Accelerations of the current state under `params` (tree + walk
+        stages, no merge, no swap: the state does not advance).  float[N, 3]
+        by body id; stats of the walk in read_stats()."""
+        p = abi.StepParams.from_buffer_copy(params)
+        p.flags |= abi.FLAG_STORE_ACCEL
+        self.reset_values(p)
+        self.partition_dead_bodies(p)
+        self.radix_sort()
+        self.build_binary_radix_tree()
+        self.compute_com_and_location()
+        self.compute_force(p)
+        return self.read_accel()[:, :3]
+
+    # ---- learned multipole-acceptance criterion ---------------------------------
+    def mac_set_weights(self, w: np.ndarray):
+        a = np.ascontiguousarray(w, dtype=np.float32).reshape(-1)
+        self._chk(lib().gbh_mac_set_weights(self._h, _ptr(a), len(a)))
+
+    def mac_get_weights(self) -> np.ndarray:
+        out = np.zeros(abi.MAC_NUM_PARAMS, dtype=np.float32)
+        self._chk(lib().gbh_mac_get_weights(self._h, _ptr(out), len(out)))
+        return out
+
+    def mac_generate(self, params: abi.StepParams, max_pairs: int, seed: int = 0) -> int:
+        cnt = C.c_uint32(0)
+        self._chk(lib().gbh_mac_generate(self._h, C.byref(params), max_pairs, seed, C.byref(cnt)))
+        return int(cnt.value)
+
+    def mac_read_pairs(self, count: int, offset: int = 0):
+        f = np.zeros((count, abi.MAC_FEATURES), dtype=np.float32)
+        y = np.zeros(count, dtype=np.float32)
+        self._chk(lib().gbh_mac_read_pairs(self._h, _ptr(f), _ptr(y), count, offset))
+        return f, y
+
+    def mac_read_pair_ids(self, count: int, offset: int = 0) -> np.ndarray:
+        """(first sorted slot of the group, group size, node id) per pair."""
+        out = np.zeros((count, 3), dtype=np.uint32)
+        self._chk(lib().gbh_mac_read_pair_ids(self._h, _ptr(out), count, offset))
+        return out
+
+    def mac_write_pairs(self, features: np.ndarray, labels: np.ndarray):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        y = np.ascontiguousarray(labels, dtype=np.float32)
+        self._chk(lib().gbh_mac_write_pairs(self._h, _ptr(f), _ptr(y), len(y)))
+
+    def mac_train(self, epochs: int, batch: int = 8192, lr: float = 3e-3, seed: int = 0) -> np.ndarray:
+        losses = np.zeros(epochs, dtype=np.float32)
+        self._chk(lib().gbh_mac_train(self._h, epochs, batch, lr, seed, _ptr(losses)))
+        return losses
+
+    def mac_loss_grad(self, features: np.ndarray, labels: np.ndarray):
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        y = np.ascontiguousarray(labels, dtype=np.float32)
+        loss = C.c_float(0)
+        grad = np.zeros(abi.MAC_NUM_PARAMS, dtype=np.float32)
+        self._chk(lib().gbh_mac_loss_grad(self._h, _ptr(f), _ptr(y), len(y), C.byref(loss), _ptr(grad)))
+        return float(loss.value), grad
+
+    def mac_predict(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, dtype=np.float32)
+        out = np.zeros(len(f), dtype=np.float32)
+        self._chk(lib().gbh_mac_predict(self._h, _ptr(f), len(f), _ptr(out)))
+        return out

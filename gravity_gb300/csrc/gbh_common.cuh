@@ -13,6 +13,7 @@
 #define GBH_NONE 0xFFFFFFFFu
 #define GBH_WARP 32
 #define GBH_WALK_STACK 192     // per-warp walk stack entries (tree height + 1 needed)
+#define GBH_GROUP_MAX 32       // bodies per group of the group walk (one warp)
 #define GBH_MAX_TREE_HEIGHT_REF 64  // the reference fills 64 levels (GPU.java:41)
 
 // onesweep radix sort geometry (8-bit digits, 8 passes over the 63-bit key)
@@ -58,7 +59,8 @@ struct DevState {
     uint32_t max_stack;
     uint32_t merge_tasks;
     uint32_t sort_tiles[SORT_PASSES];  // onesweep tile tickets
-    uint32_t pad[2];
+    uint32_t num_groups;               // body groups of the group walk
+    uint32_t frontier_saturated;       // group walks that accepted instead of opening (full stack)
     unsigned long long interactions;
     unsigned long long opened;
     unsigned long long mac_evals;
@@ -94,6 +96,9 @@ struct StepBuffers {
     uint32_t* locks;
     uint32_t* conflicts;
     float4* accel;
+    float* accel_mag;     // |acceleration| of the last walk, by body id (learned MAC feature)
+    uint32_t* node_lo;    // first sorted slot of each internal node's leaf range
+    uint2* groups;        // (first slot, body count) of the group walk's body groups
     // compaction scratch
     uint32_t* tile_dead;
     float* tile_aabb;
@@ -176,6 +181,32 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
+}
+
+// Symplectic update and static bounds of one body after its walk
+// (bh_force.comp:117-141); writes the output body buffer.
+__device__ __forceinline__ void walk_update(const StepBuffers& b, const gbh_step_params* P, const gbh_sim_values* sim,
+                                            uint32_t bi, float4 pm, float4 vd, float ax, float ay, float az) {
+    const float dt = P->dt;
+    const float nvx = vd.x + ax * dt, nvy = vd.y + ay * dt, nvz = vd.z + az * dt;
+    float npx = pm.x + nvx * dt, npy = pm.y + nvy * dt, npz = pm.z + nvz * dt;
+    if (P->static_or_dynamic == GBH_BOUNDS_STATIC) {
+        const float* mn = sim->bounds_min;
+        const float* mx = sim->bounds_max;
+        if (P->wrap_around) {
+            float x, y;
+            x = npx - mn[0]; y = mx[0] - mn[0]; npx = (x - y * floorf(x / y)) + mn[0];
+            x = npy - mn[1]; y = mx[1] - mn[1]; npy = (x - y * floorf(x / y)) + mn[1];
+            x = npz - mn[2]; y = mx[2] - mn[2]; npz = (x - y * floorf(x / y)) + mn[2];
+        } else if (pm.x < mn[0] || pm.x > mx[0] || pm.y < mn[1] || pm.y > mx[1] || pm.z < mn[2] || pm.z > mx[2]) {
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            st_body(b.bodies_out, bi, z, z);
+            atomicAdd(&b.sim->out_of_bounds, 1u);
+            atomicAdd(&b.st->oob, 1u);
+            return;
+        }
+    }
+    st_body(b.bodies_out, bi, make_float4(npx, npy, npz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
 }
 
 // ---- launchers (host), one translation unit each -----------------------------

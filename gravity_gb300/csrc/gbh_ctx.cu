@@ -72,6 +72,9 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.locks = c->locks;
     b.conflicts = c->conflicts;
     b.accel = c->accel;
+    b.accel_mag = c->accel_mag;
+    b.node_lo = c->node_lo;
+    b.groups = c->groups;
     b.tile_dead = c->tile_dead;
     b.tile_aabb = c->tile_aabb;
     b.hist = c->hist;
@@ -157,8 +160,10 @@ static int upload_params(gbh_ctx* c, const gbh_step_params* p) {
     if (p->merging_collision_or_neither > 2 || p->static_or_dynamic > 1 || p->mac_mode > 2 || p->precision_mode > 1)
         return fail(c, GBH_ERR_INVALID, "step params: enum out of range");
     if ((p->flags & GBH_FLAG_STORE_ACCEL) && !c->accel) return fail(c, GBH_ERR_INVALID, "accel buffer missing");
-    if (p->mac_mode != GBH_MAC_PLAIN && !c->mac_ready && p->mac_mode == GBH_MAC_LEARNED)
+    if (p->mac_mode == GBH_MAC_LEARNED && !c->mac_ready)
         return fail(c, GBH_ERR_STATE, "learned MAC selected but no weights were set");
+    if (p->mac_mode != GBH_MAC_PLAIN && p->merging_collision_or_neither != GBH_MODE_NEITHER)
+        return fail(c, GBH_ERR_UNSUPPORTED, "group and learned acceptance criteria run gravity only (no merges or collisions)");
     // pageable source: the copy is staged before cudaMemcpyAsync returns
     if (!c->params_valid || memcmp(&c->params_host, p, sizeof(*p)) != 0) {
         CUDA_TRY(c, cudaMemcpyAsync(c->params_dev, p, sizeof(*p), cudaMemcpyHostToDevice, c->stream));
@@ -210,7 +215,8 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_par = A.add(sizeof(gbh_step_params));
     size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8);
     size_t o_locks = A.add((size_t)n * 4), o_conf = A.add((size_t)n * 4);
-    size_t o_accel = A.add((size_t)n * 16);
+    size_t o_accel = A.add((size_t)n * 16), o_amag = A.add((size_t)n * 4);
+    size_t o_nlo = A.add((size_t)ni * 4), o_groups = A.add((size_t)n * 8);
     size_t o_tdead = A.add((size_t)c->prep_tiles_cap * 4), o_taabb = A.add((size_t)c->prep_tiles_cap * 24);
     size_t o_hist = A.add(SORT_PASSES * SORT_RADIX * 4), o_bbase = A.add(SORT_PASSES * SORT_RADIX * 4);
     c->lookback_bytes = (size_t)SORT_PASSES * c->sort_tiles_cap * SORT_RADIX * 4;
@@ -242,6 +248,9 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->locks = (uint32_t*)(base + o_locks);
     c->conflicts = (uint32_t*)(base + o_conf);
     c->accel = (float4*)(base + o_accel);
+    c->accel_mag = (float*)(base + o_amag);
+    c->node_lo = (uint32_t*)(base + o_nlo);
+    c->groups = (uint2*)(base + o_groups);
     c->tile_dead = (uint32_t*)(base + o_tdead);
     c->tile_aabb = (float*)(base + o_taabb);
     c->hist = (uint32_t*)(base + o_hist);
@@ -249,6 +258,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->lookback = (uint32_t*)(base + o_lb);
 
     sort_setup();
+    group_walk_setup();
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->arena, 0, A.total, c->stream);
     // SimulationValues as packed by GPU.packValues (GPU.java:1096-1143)
@@ -463,6 +473,7 @@ int gbh_read_stats(gbh_ctx* c, gbh_stats* s) {
     s->tree_height = st.tree_height;
     s->max_stack = st.max_stack;
     s->error_word = st.error_word;
+    s->frontier_saturated = st.frontier_saturated;
     return GBH_OK;
 }
 

@@ -39,6 +39,9 @@ struct gbh_ctx {
     uint32_t* locks = nullptr;
     uint32_t* conflicts = nullptr;
     float4* accel = nullptr;
+    float* accel_mag = nullptr;
+    uint32_t* node_lo = nullptr;
+    uint2* groups = nullptr;
     uint32_t* tile_dead = nullptr;
     float* tile_aabb = nullptr;
     uint32_t* hist = nullptr;
@@ -60,3 +63,4 @@ StepBuffers ctx_buffers(const gbh_ctx* c);
 int enqueue_walk_learned(gbh_ctx* c);
 void mac_release(gbh_ctx* c);
 void sort_setup();
+void group_walk_setup();

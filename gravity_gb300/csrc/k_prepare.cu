@@ -38,6 +38,7 @@ __global__ void k_reset(StepBuffers b) {
         st->interactions = 0;
         st->opened = 0;
         st->mac_evals = 0;
+        st->frontier_saturated = 0;
         // units update, bh_update.comp:22-25 / common.glsl:346-360
         if (p->units.mass != 0.0f) {
             gbh_sim_values* sim = b.sim;

@@ -72,6 +72,7 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     nd->child_a = left;
     nd->child_b = right;
     nd->node_depth = (uint32_t)mn;
+    b.node_lo[i] = (uint32_t)mn;
     nd->bodies_contained = (uint32_t)(mx - mn + 1);
     nd->ready_children = 0;
     const uint32_t self = (uint32_t)i + N;

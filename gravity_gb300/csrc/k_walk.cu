@@ -179,28 +179,8 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     }
     if (!active) return;
     if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
-
-    // symplectic update and static bounds, bh_force.comp:117-141
-    const float dt = P->dt;
-    const float nvx = vd.x + ax * dt, nvy = vd.y + ay * dt, nvz = vd.z + az * dt;
-    float npx = pm.x + nvx * dt, npy = pm.y + nvy * dt, npz = pm.z + nvz * dt;
-    if (P->static_or_dynamic == GBH_BOUNDS_STATIC) {
-        const float* mn = sim->bounds_min;
-        const float* mx = sim->bounds_max;
-        if (P->wrap_around) {
-            float x, y;
-            x = npx - mn[0]; y = mx[0] - mn[0]; npx = (x - y * floorf(x / y)) + mn[0];
-            x = npy - mn[1]; y = mx[1] - mn[1]; npy = (x - y * floorf(x / y)) + mn[1];
-            x = npz - mn[2]; y = mx[2] - mn[2]; npz = (x - y * floorf(x / y)) + mn[2];
-        } else if (pm.x < mn[0] || pm.x > mx[0] || pm.y < mn[1] || pm.y > mx[1] || pm.z < mn[2] || pm.z > mx[2]) {
-            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            st_body(b.bodies_out, bi, z, z);
-            atomicAdd(&b.sim->out_of_bounds, 1u);
-            atomicAdd(&b.st->oob, 1u);
-            return;
-        }
-    }
-    st_body(b.bodies_out, bi, make_float4(npx, npy, npz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
+    if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
+    walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
 }
 
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s) {

@@ -1,0 +1,363 @@
+// k_walk_group.cu — group walk: one acceptance decision per (32-body group, node).
+//
+// The reference decides per body (bh_force.comp:57-115).  Here a warp takes
+// one body group, a subtree of at most 32 bodies (k_find_groups), and walks
+// the tree once for all of its bodies:
+//   * candidates come off a per-warp stack 32 at a time, one per lane; each
+//     lane evaluates the acceptance criterion of the group against its node;
+//   * accepted nodes and leaves are appended to an interaction list, opened
+//     nodes push their two children;
+//   * every 32 list entries, all 32 lanes accumulate the forces of the whole
+//     list on their own body (dense FMA loop, node data broadcast from shared
+//     memory).
+// Criteria (gbh_step_params.mac_mode):
+//   GBH_MAC_GROUP    accept when half_side < theta * (|com - c_g| - R_g), with
+//                    c_g, R_g the centre and half diagonal of the group's box;
+//   GBH_MAC_LEARNED  nodes that pass the group rule at theta_g = 0.25 are
+//                    accepted, nodes that fail it at theta_g = 1 are opened,
+//                    and in between the MLP decides: accept when its predicted
+//                    log10 relative error of the monopole, max over the group,
+//                    is below mac_tolerance (mac_mlp.cuh: features and
+//                    tensor-core inference).
+// A third instance records (group, node) candidates and their features for
+// the MLP's training data (gbh_mac_generate).
+// Only gravity (merging_collision_or_neither == 0) runs here.
+#include <cstddef>
+
+#include "gbh_ctx.h"
+#include "mac_mlp.cuh"
+
+#define GW_THREADS 256
+#define GW_WARPS (GW_THREADS / 32)
+#define GW_STACK 768
+#define GW_LIST 64
+#define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
+
+enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
+
+// shared memory: the stacks and lists first, the network's tiles last (only
+// the learned walk allocates them)
+struct GroupSmem {
+    uint32_t stack[GW_WARPS][GW_STACK];
+    float4 list_cm[GW_WARPS][GW_LIST];
+    uint32_t list_id[GW_WARPS][GW_LIST];
+    // queued band candidates of the learned walk: centre of mass, box and
+    // count, box and id, children
+    float4 pend_cm[GW_WARPS][GW_QUEUE];
+    float4 pend_b0[GW_WARPS][GW_QUEUE];
+    float4 pend_b1[GW_WARPS][GW_QUEUE];
+    uint2 pend_kids[GW_WARPS][GW_QUEUE];
+    uint32_t frag[MAC_FRAG_WORDS * 32];
+    __nv_bfloat16 x[GW_WARPS * 32 * 16];  // feature tile of the batch being decided
+};
+#define GW_SMEM_THETA offsetof(GroupSmem, pend_cm)
+
+// Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
+// more (every leaf lies in exactly one).  A group is a contiguous range of
+// sorted slots, spatially compact because it is one tree node.
+__global__ void k_find_groups(StepBuffers b) {
+    const uint32_t n = b.st->n_new;
+    const uint32_t N = b.N;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n == 1) {
+        if (t == 0) {
+            b.groups[0] = make_uint2(0u, 1u);
+            b.st->num_groups = 1;
+        }
+        return;
+    }
+    if (t + 1 < n) {
+        const gbh_node* nd = &b.internal[t];
+        const uint32_t cnt = nd->bodies_contained;
+        if (cnt <= GBH_GROUP_MAX) {
+            const uint32_t p = nd->parent_id;
+            if (p == GBH_NONE || b.internal[p - N].bodies_contained > GBH_GROUP_MAX) {
+                const uint32_t slot = atomicAdd(&b.st->num_groups, 1u);
+                b.groups[slot] = make_uint2(b.node_lo[t], cnt);
+            }
+        }
+    }
+    if (t < n) {
+        const uint32_t p = b.leaf[t].parent_id;
+        if (p != GBH_NONE && b.internal[p - N].bodies_contained > GBH_GROUP_MAX) {
+            const uint32_t slot = atomicAdd(&b.st->num_groups, 1u);
+            b.groups[slot] = make_uint2(t, 1u);
+        }
+    }
+}
+
+template <int MODE>
+__global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk_group(StepBuffers b, MacDeviceWeights mw) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
+    if (MODE == GM_LEARNED) mac_load_frag(mw, S.frag, S.x);
+    const uint32_t n = b.st->n_new;
+    const uint32_t N = b.N;
+    const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+    const uint32_t num_groups = b.st->num_groups;
+    // groups hold up to 32 bodies, usually fewer: warps loop over them
+    for (uint32_t gi = blockIdx.x * GW_WARPS + w; gi < num_groups; gi += gridDim.x * GW_WARPS) {
+    const uint2 grp = b.groups[gi];
+    const uint32_t g = grp.x + lane;
+    const bool active = lane < grp.y;
+    const gbh_step_params* P = b.params;
+    const gbh_sim_values* sim = b.sim;
+    const float G = sim->gravitational_constant;
+    const float soft = P->softening, theta = P->theta, tol = P->mac_tolerance;
+    uint32_t* stk = S.stack[w];
+    float4* lcm = S.list_cm[w];
+    uint32_t* lid = S.list_id[w];
+
+    const uint32_t bi = active ? b.idx_in[g] : 0u;
+    const float4 pm = b.leaf_pm[active ? g : grp.x];
+    const float4 vd = active ? ld_vel_density(b.bodies_in, bi) : make_float4(0.f, 0.f, 0.f, 0.f);
+    // group box (inactive lanes repeat the first body)
+    float mnx = pm.x, mny = pm.y, mnz = pm.z, mxx = pm.x, mxy = pm.y, mxz = pm.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+        mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
+    }
+    GroupGeom gg;
+    gg.cx = 0.5f * (mnx + mxx);
+    gg.cy = 0.5f * (mny + mxy);
+    gg.cz = 0.5f * (mnz + mxz);
+    const float hx = 0.5f * (mxx - mnx), hy = 0.5f * (mxy - mny), hz = 0.5f * (mxz - mnz);
+    gg.R = sqrtf(hx * hx + hy * hy + hz * hz);
+    gg.bmin = make_float3(mnx, mny, mnz);
+    gg.bmax = make_float3(mxx, mxy, mxz);
+    gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi) : 0.0f;
+
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    uint32_t inter = 0, evals = 0;
+    uint32_t sp = n > 1 ? 1u : 0u, ln = 0, np = 0;
+    bool saturated = false;
+    if (lane == 0) stk[0] = N;  // root
+    __syncwarp();
+
+    // forces of list entries [0, cnt) on every lane's own body
+    auto flush = [&](uint32_t cnt) {
+#pragma unroll 4
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const float4 c = lcm[j];
+            const uint32_t lj = lid[j];
+            const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
+            const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+            const float inv = rsqrtf(rr);
+            const float f = (lj == g) ? 0.0f : G * c.w * (inv * inv * inv);
+            ax = __fmaf_rn(f, rx, ax);
+            ay = __fmaf_rn(f, ry, ay);
+            az = __fmaf_rn(f, rz, az);
+        }
+        inter += cnt;
+    };
+    // each lane's outcome: 1 list, 2 open (push children); warp-collective
+    auto commit = [&](uint32_t kind, uint32_t id, float4 cm, uint32_t ca, uint32_t cb) {
+        uint32_t bo = __ballot_sync(0xffffffffu, kind == 2);
+        if (sp + 2 * __popc(bo) > GW_STACK) {
+            // frontier full: accept instead of opening (less accurate, never wrong)
+            saturated = true;
+            if (kind == 2) kind = 1;
+            bo = 0;
+        }
+        const uint32_t bl = __ballot_sync(0xffffffffu, kind == 1);
+        if (kind == 1) {
+            const uint32_t pos = ln + __popc(bl & lanemask_lt());
+            lcm[pos] = cm;
+            lid[pos] = id;
+        }
+        ln += __popc(bl);
+        if (kind == 2) {
+            const uint32_t pos = sp + 2 * __popc(bo & lanemask_lt());
+            stk[pos] = ca;
+            stk[pos + 1] = cb;
+        }
+        sp += 2 * __popc(bo);
+        __syncwarp();
+        if (ln >= 32) {
+            flush(32);
+            ln -= 32;
+            __syncwarp();
+            if (lane < ln) {  // move the remaining entries to the front
+                lcm[lane] = lcm[32 + lane];
+                lid[lane] = lid[32 + lane];
+            }
+            __syncwarp();
+        }
+    };
+
+    // decide the first `cnt` (<= 32) queued band candidates with one MLP pass
+    // and move the rest of the queue to the front
+    auto decide_queue = [&](uint32_t cnt) {
+        // features of queue rows [0, cnt), one per lane, then one MLP pass
+        uint32_t kind = 0, id = 0, ca = 0, cb = 0;
+        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+        float feat[MAC_FEATURES];
+#pragma unroll
+        for (int q = 0; q < MAC_FEATURES; ++q) feat[q] = 0.0f;
+        if (lane < cnt) {
+            NodeGeom ng;
+            cm = S.pend_cm[w][lane];
+            const float4 b0 = S.pend_b0[w][lane];
+            const float4 b1 = S.pend_b1[w][lane];
+            ng.cm = cm;
+            ng.bmin = make_float3(b0.x, b0.y, b0.z);
+            ng.bmax = make_float3(b1.x, b1.y, b1.z);
+            ng.count = __float_as_uint(b0.w);
+            id = __float_as_uint(b1.w);
+            const uint2 kids = S.pend_kids[w][lane];
+            ca = kids.x;
+            cb = kids.y;
+            mac_features(gg, ng, G, soft, feat);
+        }
+        mac_stage_features(mw, w, lane, feat);
+        const float pred = mac_infer_warp(mw, w, lane);
+        evals += cnt;
+        if (lane < cnt) kind = pred < tol ? 1u : 2u;
+        const uint32_t rest = np - cnt;
+        __syncwarp();
+        if (lane < rest) {
+            S.pend_cm[w][lane] = S.pend_cm[w][32 + lane];
+            S.pend_b0[w][lane] = S.pend_b0[w][32 + lane];
+            S.pend_b1[w][lane] = S.pend_b1[w][32 + lane];
+            S.pend_kids[w][lane] = S.pend_kids[w][32 + lane];
+        }
+        np = rest;
+        __syncwarp();
+        commit(kind, id, cm, ca, cb);
+    };
+
+    while (sp > 0 || np > 0) {
+        if (MODE == GM_LEARNED && sp == 0) {
+            decide_queue(min(np, 32u));
+            continue;
+        }
+        const uint32_t k = min(sp, 32u);
+        sp -= k;
+        const bool has = lane < k;
+        const uint32_t id = has ? stk[sp + lane] : 0u;
+        __syncwarp();
+        uint32_t kind = 0;  // 0 nothing, 1 list, 2 open, 3 queued for the network
+        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 qb0 = cm, qb1 = cm;
+        uint32_t ca = 0, cb = 0, qcount = 0;
+        if (has) {
+            if (id < N) {
+                cm = b.leaf_pm[id];
+                kind = 1;
+            } else {
+                const gbh_node* nd = &b.internal[id - N];
+                const float4* q = reinterpret_cast<const float4*>(nd);
+                cm = __ldg(q + 0);
+                qb0 = __ldg(q + 1);
+                qb1 = __ldg(q + 2);  // aabb4, aabb5, childA, childB
+                ca = __float_as_uint(qb1.z);
+                cb = __float_as_uint(qb1.w);
+                qcount = __ldg(&nd->bodies_contained);
+                NodeGeom ng;
+                ng.cm = cm;
+                ng.bmin = make_float3(qb0.x, qb0.y, qb0.z);
+                ng.bmax = make_float3(qb0.w, qb1.x, qb1.y);
+                ng.count = qcount;
+                if (MODE == GM_LEARNED) {
+                    // the network decides the band between a rule that is
+                    // safe to accept (theta_g = 0.25) and one that must open
+                    // (theta_g = 1): it never accepts a node the group reaches
+                    if (group_theta_accept(gg, ng, MAC_BAND_LO))
+                        kind = 1;
+                    else if (group_theta_accept(gg, ng, MAC_BAND_HI))
+                        kind = 3;
+                    else
+                        kind = 2;
+                } else {
+                    kind = group_theta_accept(gg, ng, theta) ? 1 : 2;
+                    // training pairs: the band the network decides (see GM_LEARNED)
+                    if (MODE == GM_RECORD && ng.count <= mw.rec_max_bodies &&
+                        (hash32(id ^ hash32(gi + mw.rec_seed)) & 1023u) < mw.rec_keep &&
+                        group_theta_accept(gg, ng, MAC_BAND_HI) && !group_theta_accept(gg, ng, MAC_BAND_LO)) {
+                        const uint32_t slot = atomicAdd(mw.rec_count, 1u);
+                        if (slot < mw.rec_cap) {
+                            float f[MAC_FEATURES];
+                            mac_features(gg, ng, G, soft, f);
+                            mw.rec_pairs[slot] = make_uint2(gi, id);
+#pragma unroll
+                            for (int q = 0; q < MAC_FEATURES; ++q) mw.rec_feats[(size_t)slot * MAC_FEATURES + q] = f[q];
+                        }
+                    }
+                }
+            }
+        }
+        if (MODE == GM_LEARNED) {
+            // queue band candidates with their geometry; the network decides
+            // them 32 at a time
+            const uint32_t bq = __ballot_sync(0xffffffffu, kind == 3);
+            if (kind == 3) {
+                const uint32_t row = np + __popc(bq & lanemask_lt());
+                S.pend_cm[w][row] = cm;
+                S.pend_b0[w][row] = make_float4(qb0.x, qb0.y, qb0.z, __uint_as_float(qcount));
+                S.pend_b1[w][row] = make_float4(qb0.w, qb1.x, qb1.y, __uint_as_float(id));
+                S.pend_kids[w][row] = make_uint2(ca, cb);
+                kind = 0;
+            }
+            np += __popc(bq);
+            __syncwarp();
+        } else {
+            evals += __popc(__ballot_sync(0xffffffffu, has && id >= N));
+        }
+        commit(kind, id, cm, ca, cb);
+        if (MODE == GM_LEARNED && np >= 32) decide_queue(32);
+    }
+    if (ln) flush(ln);
+    (void)saturated;
+
+    // counters: interactions count the active lanes of every list entry
+    const uint32_t act = __popc(__ballot_sync(0xffffffffu, active));
+    if (lane == 0) {
+        atomicAdd(&b.st->interactions, (unsigned long long)inter * act);
+        atomicAdd(&b.st->mac_evals, (unsigned long long)evals);
+    }
+    if (active) {
+        if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
+        if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
+        walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
+    }
+    __syncwarp();
+    }  // groups
+}
+
+static size_t group_smem(int mode) { return mode == GM_LEARNED ? sizeof(GroupSmem) : GW_SMEM_THETA; }
+
+void group_walk_setup() {
+    cudaFuncSetAttribute(k_walk_group<GM_THETA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(GM_THETA));
+    cudaFuncSetAttribute(k_walk_group<GM_LEARNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)group_smem(GM_LEARNED));
+    cudaFuncSetAttribute(k_walk_group<GM_RECORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(GM_RECORD));
+}
+
+void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
+    cudaMemsetAsync(&b.st->num_groups, 0, 4, s);
+    k_find_groups<<<(b.N + 255) / 256, 256, 0, s>>>(b);
+}
+
+template <int MODE>
+static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
+    if (MODE != GM_RECORD) launch_find_groups(b, s);
+    const uint32_t blocks = (b.N + GW_THREADS - 1) / GW_THREADS;
+    k_walk_group<MODE><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
+}
+
+void launch_walk_group(const StepBuffers& b, const MacDeviceWeights& mw, bool learned, cudaStream_t s) {
+    if (learned)
+        launch_mode<GM_LEARNED>(b, mw, s);
+    else
+        launch_mode<GM_THETA>(b, mw, s);
+}
+
+// the caller runs launch_find_groups once first: pairs name groups by index
+void launch_walk_group_record(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
+    launch_mode<GM_RECORD>(b, mw, s);
+}

@@ -167,7 +167,8 @@ typedef struct gbh_stats {
     uint32_t tree_height;    /* height of the root */
     uint32_t max_stack;      /* deepest walk stack seen */
     uint32_t error_word;     /* GBH_DEVERR_* bits, sticky until gbh_clear_error */
-    uint32_t pad;
+    uint32_t frontier_saturated; /* group walks whose candidate stack filled up: nodes were
+                                    accepted instead of opened (less accurate, still a valid sum) */
 } gbh_stats;
 
 /* Device pointers of the live buffers, for headless consumers that replace the
@@ -289,6 +290,9 @@ int gbh_mac_get_weights(gbh_ctx* ctx, float* params, uint32_t count);
 int gbh_mac_generate(gbh_ctx* ctx, const gbh_step_params* params, uint32_t max_pairs,
                      uint64_t seed, uint32_t* out_count);
 int gbh_mac_read_pairs(gbh_ctx* ctx, float* features, float* labels, uint32_t count, uint32_t offset);
+/* Group and node of each generated pair, uint32_t[3] per pair: the group's
+ * first sorted slot, its body count, and the node's global id. */
+int gbh_mac_read_pair_ids(gbh_ctx* ctx, uint32_t* slot_count_node, uint32_t count, uint32_t offset);
 int gbh_mac_write_pairs(gbh_ctx* ctx, const float* features, const float* labels, uint32_t count);
 /* Train the MLP on the stored pairs with Adam (hand-written forward, backward
  * and Adam kernels; BF16 tensor-core matmuls, FP32 master weights).

@@ -1,0 +1,119 @@
+"""The learned multipole-acceptance criterion on the GPU: the tensor-core
+forward pass and the hand-written backward pass against the CPU oracle
+(oracle/mac_oracle.py), the training-pair labels against a float64
+recomputation, training, and the learned walk against the group theta rule
+at equal p99 acceleration error."""
+import numpy as np
+import pytest
+
+from gravity_gb300 import BarnesHut, abi, accuracy, ic
+from oracle import mac_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(bodies):
+    sim = BarnesHut(len(bodies), ic.exact_bounds(bodies), abi.units(G=1.0))
+    sim.upload_bodies(bodies)
+    sim.init()
+    return sim
+
+
+def test_mac_forward_and_gradient_match_cpu(gbh_lib):
+    sim = _sim(ic.plummer(1024, seed=1))
+    rng = np.random.default_rng(3)
+    p = rng.normal(0, 0.3, M.NPARAMS).astype(np.float32)
+    x = rng.normal(0, 1, (2000, M.F)).astype(np.float32)
+    t = rng.normal(-3, 1, 2000).astype(np.float32)
+    sim.mac_set_weights(p)
+    assert np.array_equal(sim.mac_get_weights(), p)
+    pred = sim.mac_predict(x)
+    ref, _ = M.forward(p, x)
+    # FP32 (GPU) vs float64 (CPU) sums can round a hidden unit to a neighbouring BF16 value
+    assert np.median(np.abs(pred - ref)) < 2e-3
+    np.testing.assert_allclose(pred, ref, rtol=3e-2, atol=3e-2)
+    loss, grad = sim.mac_loss_grad(x, t)
+    rloss, rgrad = M.loss_grad(p, x, t)
+    assert abs(loss - rloss) <= 1e-3 * rloss
+    rel = np.linalg.norm(grad - rgrad) / np.linalg.norm(rgrad)
+    assert rel < 2e-2, rel
+
+
+def test_group_walk_runs_and_is_accurate(gbh_lib):
+    bodies = ic.plummer(65536, seed=2)
+    sim = _sim(bodies)
+    p = abi.step_params(theta=0.5, softening=1e-4)
+    judge = accuracy.Judge(sim, p, count=2048, seed=1)
+    plain = accuracy.evaluate(sim, judge, p)
+    g3 = accuracy.evaluate(sim, judge, abi.step_params(theta=0.3, softening=1e-4, mac=abi.MAC_GROUP))
+    g8 = accuracy.evaluate(sim, judge, abi.step_params(theta=0.8, softening=1e-4, mac=abi.MAC_GROUP))
+    assert sim.read_stats().error_word == 0
+    assert g3["p99"] < g8["p99"]
+    assert g3["interactions"] > g8["interactions"]
+    assert g3["median"] < 1e-2 and plain["median"] < 1e-1
+    # a full step with the group rule advances the state like any step
+    sim.step(abi.step_params(theta=0.5, softening=1e-4, mac=abi.MAC_GROUP))
+    sim.synchronize()
+
+
+def _label_numpy(sim, pair, accel, idx, leaves, internal, soft):
+    """log10 max_i |monopole - exact subtree sum| / |a_i| over the group's bodies."""
+    N = sim.n
+    lo_g, cnt_g, node = int(pair[0]), int(pair[1]), int(pair[2])
+    nd = internal[node - N]
+    cnt = int(nd["bodies_contained"])
+    k = node
+    while k >= N:
+        k = int(internal[k - N]["child_a"])
+    lo = k
+    sub = leaves[lo : lo + cnt]["com_mass"].astype(np.float64)
+    cm = nd["com_mass"].astype(np.float64)
+    worst = 0.0
+    for s in range(lo_g, lo_g + cnt_g):
+        x = leaves[s]["com_mass"][:3].astype(np.float64)
+        r = sub[:, :3] - x
+        w = np.ones(cnt)
+        if lo <= s < lo + cnt:
+            w[s - lo] = 0.0
+        inv3 = (np.sum(r * r, axis=1) + soft) ** -1.5
+        exact = np.sum((w * sub[:, 3] * inv3)[:, None] * r, axis=0)
+        rc = cm[:3] - x
+        mono = cm[3] * rc / (rc @ rc + soft) ** 1.5
+        a = np.linalg.norm(accel[idx[s]])
+        worst = max(worst, np.linalg.norm(mono - exact) / a)
+    return np.log10(max(worst, 1e-12))
+
+
+def test_learned_mac_pipeline_and_gain(gbh_lib):
+    soft = 0.005 ** 2
+    bodies = ic.plummer_uniform(262144, seed=3)
+    sim = _sim(bodies)
+    p = abi.step_params(theta=0.5, softening=soft)
+    count = sim.mac_generate(p, max_pairs=2_000_000, seed=1)
+    assert count > 50_000
+    feats, labels = sim.mac_read_pairs(count)
+    assert np.all(np.isfinite(feats)) and np.all(np.isfinite(labels))
+    # labels against a float64 recomputation
+    ids = sim.mac_read_pair_ids(count)
+    accel = sim.read_accel()[:, :3].astype(np.float64)
+    idx = sim.read_index()
+    leaves = sim.read_leaf_nodes()
+    internal = sim.read_internal_nodes()
+    rng = np.random.default_rng(0)
+    for j in rng.choice(count, 12, replace=False):
+        want = _label_numpy(sim, ids[j], accel, idx, leaves, internal, soft)
+        assert abs(labels[j] - want) < 0.05, (j, labels[j], want)
+    losses = sim.mac_train(epochs=6, batch=8192, lr=3e-3, seed=0)
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.6 * losses[0], losses
+    # the trained criterion against the group theta rule at the plain rule's p99
+    judge = accuracy.Judge(sim, p, count=2048, seed=2)
+    target = accuracy.evaluate(sim, judge, p)["p99"]
+    best_l, res_l = accuracy.match_p99(
+        sim, judge, lambda t: abi.step_params(theta=0.5, softening=soft, mac=abi.MAC_LEARNED, mac_tolerance=t),
+        [-4.0, -3.5, -3.0, -2.75, -2.5, -2.25, -2.0, -1.75, -1.5, -1.25, -1.0], target)
+    best_g, res_g = accuracy.match_p99(
+        sim, judge, lambda t: abi.step_params(theta=t, softening=soft, mac=abi.MAC_GROUP),
+        [0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.2], target)
+    assert best_l is not None and best_g is not None, (res_l, res_g)
+    assert best_l[1]["interactions"] < best_g[1]["interactions"], (best_l, best_g)
