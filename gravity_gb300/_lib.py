@@ -58,6 +58,8 @@ def _declare(L):
         "gbh_direct_sum": [vp, sp, vp, u32, vp],
         "gbh_mac_set_weights": [vp, vp, u32],
         "gbh_mac_get_weights": [vp, vp, u32],
+        "gbh_mac_set_band": [vp, C.c_float, C.c_float],
+        "gbh_mac_get_band": [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)],
         "gbh_mac_generate": [vp, sp, u32, u64, C.POINTER(u32)],
         "gbh_mac_read_pairs": [vp, vp, vp, u32, u32],
         "gbh_mac_write_pairs": [vp, vp, vp, u32],

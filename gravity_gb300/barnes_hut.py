@@ -229,6 +229,15 @@ class BarnesHut:
         self._chk(lib().gbh_mac_get_weights(self._h, _ptr(out), len(out)))
         return out
 
+    def mac_set_band(self, theta_accept: float, theta_open: float):
+        """Group-rule thetas bounding the band the network decides."""
+        self._chk(lib().gbh_mac_set_band(self._h, theta_accept, theta_open))
+
+    def mac_get_band(self) -> tuple[float, float]:
+        lo, hi = C.c_float(0), C.c_float(0)
+        self._chk(lib().gbh_mac_get_band(self._h, C.byref(lo), C.byref(hi)))
+        return float(lo.value), float(hi.value)
+
     def mac_generate(self, params: abi.StepParams, max_pairs: int, seed: int = 0) -> int:
         cnt = C.c_uint32(0)
         self._chk(lib().gbh_mac_generate(self._h, C.byref(params), max_pairs, seed, C.byref(cnt)))

@@ -50,6 +50,8 @@ struct MacState {
     float* labels = nullptr;   // [cap]
     uint2* pairs = nullptr;    // [cap] (group, node)
     uint32_t* count = nullptr; // device counter
+    float* band = nullptr;     // device [2]: the learned walk's band (group-rule thetas)
+    float band_host[2] = {MAC_BAND_LO, MAC_BAND_HI};
     uint32_t cap = 0;
     uint32_t num_pairs = 0;
     uint64_t adam_t = 0;
@@ -95,7 +97,7 @@ __global__ void k_mac_build_frag(const float* __restrict__ p, uint32_t* __restri
 // inference over stored features (one warp per 32 rows)
 __global__ void k_mac_predict(const float* __restrict__ feats, uint32_t n, float* __restrict__ out,
                               MacDeviceWeights mw) {
-    __shared__ uint32_t s_frag[MAC_FRAG_WORDS * 32];
+    __shared__ __align__(16) uint32_t s_frag[MAC_SMEM_FRAG_WORDS];
     __shared__ __nv_bfloat16 s_x[MAC_TRAIN_WARPS * 32 * 16];
     mac_load_frag(mw, s_frag, s_x);
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
@@ -203,7 +205,7 @@ __global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, cons
 // ---------------------------------------------------------------------------
 // training: forward (tensor cores) + backward (FP32) of 32 samples per warp
 struct TrainSmem {
-    uint32_t frag[MAC_FRAG_WORDS * 32];
+    alignas(16) uint32_t frag[MAC_SMEM_FRAG_WORDS];
     __nv_bfloat16 x[MAC_TRAIN_WARPS * 32 * 16];
     float h1[MAC_TRAIN_WARPS][32][33];
     float h2[MAC_TRAIN_WARPS][32][33];
@@ -344,6 +346,8 @@ static int mac_ensure(gbh_ctx* c) {
     MTRY(c, cudaMalloc(&m->frag, MAC_FRAG_WORDS * 32 * 4));
     MTRY(c, cudaMalloc(&m->loss, 16));
     MTRY(c, cudaMalloc(&m->count, 4));
+    MTRY(c, cudaMalloc(&m->band, 8));
+    MTRY(c, cudaMemcpyAsync(m->band, m->band_host, 8, cudaMemcpyHostToDevice, c->stream));
     MTRY(c, cudaMemsetAsync(m->grad, 0, MAC_NPARAMS * 4, c->stream));
     MTRY(c, cudaMemsetAsync(m->adam_m, 0, MAC_NPARAMS * 4, c->stream));
     MTRY(c, cudaMemsetAsync(m->adam_v, 0, MAC_NPARAMS * 4, c->stream));
@@ -378,6 +382,7 @@ void mac_release(gbh_ctx* c) {
     cudaFree(m->frag);
     cudaFree(m->loss);
     cudaFree(m->count);
+    cudaFree(m->band);
     cudaFree(m->feats);
     cudaFree(m->labels);
     cudaFree(m->pairs);
@@ -389,6 +394,7 @@ static MacDeviceWeights mac_weights(const gbh_ctx* c) {
     MacDeviceWeights mw;
     memset(&mw, 0, sizeof(mw));
     mw.frag = c->mac ? c->mac->frag : nullptr;
+    mw.band = c->mac ? c->mac->band : nullptr;
     return mw;
 }
 
@@ -419,6 +425,27 @@ int gbh_mac_set_weights(gbh_ctx* c, const float* params, uint32_t count) {
     MTRY(c, cudaGetLastError());
     MTRY(c, cudaStreamSynchronize(c->stream));
     c->mac_ready = true;
+    return GBH_OK;
+}
+
+int gbh_mac_set_band(gbh_ctx* c, float theta_accept, float theta_open) {
+    if (!c) return GBH_ERR_INVALID;
+    if (!(theta_accept > 0.0f) || !(theta_open >= theta_accept) || !(theta_open < 1e30f))
+        return mac_fail(c, GBH_ERR_INVALID, "band needs 0 < theta_accept <= theta_open");
+    MTRY(c, cudaSetDevice(c->device));
+    int rc = mac_ensure(c);
+    if (rc) return rc;
+    c->mac->band_host[0] = theta_accept;
+    c->mac->band_host[1] = theta_open;
+    MTRY(c, cudaMemcpyAsync(c->mac->band, c->mac->band_host, 8, cudaMemcpyHostToDevice, c->stream));
+    MTRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_mac_get_band(gbh_ctx* c, float* theta_accept, float* theta_open) {
+    if (!c || !theta_accept || !theta_open) return GBH_ERR_INVALID;
+    *theta_accept = c->mac ? c->mac->band_host[0] : MAC_BAND_LO;
+    *theta_open = c->mac ? c->mac->band_host[1] : MAC_BAND_HI;
     return GBH_OK;
 }
 

@@ -13,8 +13,9 @@
 // Criteria (gbh_step_params.mac_mode):
 //   GBH_MAC_GROUP    accept when half_side < theta * (|com - c_g| - R_g), with
 //                    c_g, R_g the centre and half diagonal of the group's box;
-//   GBH_MAC_LEARNED  nodes that pass the group rule at theta_g = 0.25 are
-//                    accepted, nodes that fail it at theta_g = 1 are opened,
+//   GBH_MAC_LEARNED  nodes that pass the group rule at the band's lower theta
+//                    (default 0.25) are accepted, nodes that fail it at its
+//                    upper theta (default 1) are opened (gbh_mac_set_band),
 //                    and in between the MLP decides: accept when its predicted
 //                    log10 relative error of the monopole, max over the group,
 //                    is below mac_tolerance (mac_mlp.cuh: features and
@@ -36,10 +37,12 @@
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 
 // shared memory: the stacks and lists first, the network's tiles last (only
-// the learned walk allocates them)
+// the learned walk allocates them).  The learned walk's stacks are shorter so
+// that three blocks fit on an SM.
+template <int STACK>
 struct GroupSmem {
-    uint32_t stack[GW_WARPS][GW_STACK];
-    float4 list_cm[GW_WARPS][GW_LIST];
+    uint32_t stack[GW_WARPS][STACK];
+    float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
     uint32_t list_id[GW_WARPS][GW_LIST];
     // queued band candidates of the learned walk: centre of mass, box and
     // count, box and id, children
@@ -47,10 +50,17 @@ struct GroupSmem {
     float4 pend_b0[GW_WARPS][GW_QUEUE];
     float4 pend_b1[GW_WARPS][GW_QUEUE];
     uint2 pend_kids[GW_WARPS][GW_QUEUE];
-    uint32_t frag[MAC_FRAG_WORDS * 32];
+    GroupGeom geom[GW_WARPS];  // the group's geometry and feature terms
+    alignas(16) uint32_t frag[MAC_SMEM_FRAG_WORDS];
     __nv_bfloat16 x[GW_WARPS * 32 * 16];  // feature tile of the batch being decided
 };
-#define GW_SMEM_THETA offsetof(GroupSmem, pend_cm)
+#define GW_STACK_LEARNED 640
+template <int MODE>
+struct GroupCfg {
+    static constexpr int stack = MODE == GM_LEARNED ? GW_STACK_LEARNED : GW_STACK;
+    using Smem = GroupSmem<stack>;
+    static constexpr size_t smem = MODE == GM_LEARNED ? sizeof(Smem) : offsetof(Smem, pend_cm);
+};
 
 // Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
 // more (every leaf lies in exactly one).  A group is a contiguous range of
@@ -87,10 +97,13 @@ __global__ void k_find_groups(StepBuffers b) {
 }
 
 template <int MODE>
-__global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk_group(StepBuffers b, MacDeviceWeights mw) {
+__global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_group(StepBuffers b, MacDeviceWeights mw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    GroupSmem& S = *reinterpret_cast<GroupSmem*>(smem_raw);
+    using Cfg = GroupCfg<MODE>;
+    typename Cfg::Smem& S = *reinterpret_cast<typename Cfg::Smem*>(smem_raw);
     if (MODE == GM_LEARNED) mac_load_frag(mw, S.frag, S.x);
+    const float band_lo = (MODE != GM_THETA) ? mw.band[0] : 0.0f;
+    const float band_hi = (MODE != GM_THETA) ? mw.band[1] : 0.0f;
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
@@ -110,7 +123,6 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
 
     const uint32_t bi = active ? b.idx_in[g] : 0u;
     const float4 pm = b.leaf_pm[active ? g : grp.x];
-    const float4 vd = active ? ld_vel_density(b.bodies_in, bi) : make_float4(0.f, 0.f, 0.f, 0.f);
     // group box (inactive lanes repeat the first body)
     float mnx = pm.x, mny = pm.y, mnz = pm.z, mxx = pm.x, mxy = pm.y, mxz = pm.z;
 #pragma unroll
@@ -131,34 +143,57 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
     gg.bmin = make_float3(mnx, mny, mnz);
     gg.bmax = make_float3(mxx, mxy, mxz);
     gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi) : 0.0f;
+    if (MODE != GM_THETA) group_feature_terms(gg, G, soft);
+    if (MODE == GM_LEARNED) {
+        // the features read the group's terms from shared memory
+        __syncwarp();
+        if (lane == 0) S.geom[w] = gg;
+        __syncwarp();
+    }
 
     float ax = 0.f, ay = 0.f, az = 0.f;
-    uint32_t inter = 0, evals = 0;
+    uint32_t inter = 0, evals = 0, opened = 0;
     uint32_t sp = n > 1 ? 1u : 0u, ln = 0, np = 0;
     bool saturated = false;
     if (lane == 0) stk[0] = N;  // root
     __syncwarp();
 
-    // forces of list entries [0, cnt) on every lane's own body
+    // forces of list entries [0, cnt) on every lane's own body.  With a
+    // softening of at least 1e-20 a body's own entry adds exactly zero (its
+    // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
+    const bool self_check = !(soft >= 1e-20f);
     auto flush = [&](uint32_t cnt) {
+        if (self_check) {
 #pragma unroll 4
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const float4 c = lcm[j];
-            const uint32_t lj = lid[j];
-            const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
-            const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-            const float inv = rsqrtf(rr);
-            const float f = (lj == g) ? 0.0f : G * c.w * (inv * inv * inv);
-            ax = __fmaf_rn(f, rx, ax);
-            ay = __fmaf_rn(f, ry, ay);
-            az = __fmaf_rn(f, rz, az);
+            for (uint32_t j = 0; j < cnt; ++j) {
+                const float4 c = lcm[j];
+                const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
+                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                const float inv = rsqrtf(rr);
+                const float f = (lid[j] == g) ? 0.0f : c.w * (inv * inv * inv);
+                ax = __fmaf_rn(f, rx, ax);
+                ay = __fmaf_rn(f, ry, ay);
+                az = __fmaf_rn(f, rz, az);
+            }
+        } else {
+#pragma unroll 4
+            for (uint32_t j = 0; j < cnt; ++j) {
+                const float4 c = lcm[j];
+                const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
+                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                const float inv = rsqrtf(rr);
+                const float f = c.w * (inv * inv * inv);
+                ax = __fmaf_rn(f, rx, ax);
+                ay = __fmaf_rn(f, ry, ay);
+                az = __fmaf_rn(f, rz, az);
+            }
         }
         inter += cnt;
     };
     // each lane's outcome: 1 list, 2 open (push children); warp-collective
     auto commit = [&](uint32_t kind, uint32_t id, float4 cm, uint32_t ca, uint32_t cb) {
         uint32_t bo = __ballot_sync(0xffffffffu, kind == 2);
-        if (sp + 2 * __popc(bo) > GW_STACK) {
+        if (sp + 2 * __popc(bo) > (uint32_t)Cfg::stack) {
             // frontier full: accept instead of opening (less accurate, never wrong)
             saturated = true;
             if (kind == 2) kind = 1;
@@ -167,7 +202,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
         const uint32_t bl = __ballot_sync(0xffffffffu, kind == 1);
         if (kind == 1) {
             const uint32_t pos = ln + __popc(bl & lanemask_lt());
-            lcm[pos] = cm;
+            lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
             lid[pos] = id;
         }
         ln += __popc(bl);
@@ -177,6 +212,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
             stk[pos + 1] = cb;
         }
         sp += 2 * __popc(bo);
+        opened += __popc(bo);
         __syncwarp();
         if (ln >= 32) {
             flush(32);
@@ -194,30 +230,33 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
     // and move the rest of the queue to the front
     auto decide_queue = [&](uint32_t cnt) {
         // features of queue rows [0, cnt), one per lane, then one MLP pass
-        uint32_t kind = 0, id = 0, ca = 0, cb = 0;
-        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
         float feat[MAC_FEATURES];
 #pragma unroll
         for (int q = 0; q < MAC_FEATURES; ++q) feat[q] = 0.0f;
         if (lane < cnt) {
             NodeGeom ng;
-            cm = S.pend_cm[w][lane];
+            ng.cm = S.pend_cm[w][lane];
             const float4 b0 = S.pend_b0[w][lane];
             const float4 b1 = S.pend_b1[w][lane];
-            ng.cm = cm;
             ng.bmin = make_float3(b0.x, b0.y, b0.z);
             ng.bmax = make_float3(b1.x, b1.y, b1.z);
             ng.count = __float_as_uint(b0.w);
-            id = __float_as_uint(b1.w);
-            const uint2 kids = S.pend_kids[w][lane];
-            ca = kids.x;
-            cb = kids.y;
-            mac_features(gg, ng, G, soft, feat);
+            mac_features(S.geom[w], ng, feat);
         }
         mac_stage_features(mw, w, lane, feat);
         const float pred = mac_infer_warp(mw, w, lane);
         evals += cnt;
-        if (lane < cnt) kind = pred < tol ? 1u : 2u;
+        // the row's node, read back after the network (fewer live registers)
+        uint32_t kind = 0, id = 0, ca = 0, cb = 0;
+        float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < cnt) {
+            kind = pred < tol ? 1u : 2u;
+            cm = S.pend_cm[w][lane];
+            id = __float_as_uint(S.pend_b1[w][lane].w);
+            const uint2 kids = S.pend_kids[w][lane];
+            ca = kids.x;
+            cb = kids.y;
+        }
         const uint32_t rest = np - cnt;
         __syncwarp();
         if (lane < rest) {
@@ -265,24 +304,21 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
                 ng.count = qcount;
                 if (MODE == GM_LEARNED) {
                     // the network decides the band between a rule that is
-                    // safe to accept (theta_g = 0.25) and one that must open
-                    // (theta_g = 1): it never accepts a node the group reaches
-                    if (group_theta_accept(gg, ng, MAC_BAND_LO))
-                        kind = 1;
-                    else if (group_theta_accept(gg, ng, MAC_BAND_HI))
-                        kind = 3;
-                    else
-                        kind = 2;
+                    // safe to accept (band_lo, default theta_g = 0.25) and one
+                    // that must open (band_hi, default theta_g = 1): it never
+                    // accepts a node the group reaches
+                    const float rho = group_rho(gg, ng);
+                    kind = rho < band_lo ? 1u : rho < band_hi ? 3u : 2u;
                 } else {
                     kind = group_theta_accept(gg, ng, theta) ? 1 : 2;
                     // training pairs: the band the network decides (see GM_LEARNED)
                     if (MODE == GM_RECORD && ng.count <= mw.rec_max_bodies &&
                         (hash32(id ^ hash32(gi + mw.rec_seed)) & 1023u) < mw.rec_keep &&
-                        group_theta_accept(gg, ng, MAC_BAND_HI) && !group_theta_accept(gg, ng, MAC_BAND_LO)) {
+                        group_rho(gg, ng) < band_hi && !(group_rho(gg, ng) < band_lo)) {
                         const uint32_t slot = atomicAdd(mw.rec_count, 1u);
                         if (slot < mw.rec_cap) {
                             float f[MAC_FEATURES];
-                            mac_features(gg, ng, G, soft, f);
+                            mac_features(gg, ng, f);
                             mw.rec_pairs[slot] = make_uint2(gi, id);
 #pragma unroll
                             for (int q = 0; q < MAC_FEATURES; ++q) mw.rec_feats[(size_t)slot * MAC_FEATURES + q] = f[q];
@@ -319,17 +355,22 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_LEARNED ? 2 : 3) void k_walk
     if (lane == 0) {
         atomicAdd(&b.st->interactions, (unsigned long long)inter * act);
         atomicAdd(&b.st->mac_evals, (unsigned long long)evals);
+        atomicAdd(&b.st->opened, (unsigned long long)opened);
     }
     if (active) {
         if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
         if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
+        const float4 vd = ld_vel_density(b.bodies_in, bi);
         walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
     }
     __syncwarp();
     }  // groups
 }
 
-static size_t group_smem(int mode) { return mode == GM_LEARNED ? sizeof(GroupSmem) : GW_SMEM_THETA; }
+static size_t group_smem(int mode) {
+    return mode == GM_LEARNED ? GroupCfg<GM_LEARNED>::smem : mode == GM_RECORD ? GroupCfg<GM_RECORD>::smem
+                                                                              : GroupCfg<GM_THETA>::smem;
+}
 
 void group_walk_setup() {
     cudaFuncSetAttribute(k_walk_group<GM_THETA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(GM_THETA));

@@ -38,14 +38,24 @@
 #define MAC_FRAG_B1 8    // 4 n-tiles x 2 columns
 #define MAC_FRAG_B2 8
 #define MAC_FRAG_WORDS (MAC_FRAG_W1 + MAC_FRAG_W2 + MAC_FRAG_W3 + MAC_FRAG_B1 + MAC_FRAG_B2 + 1)
+// In shared memory the table is stored in 16-byte chunks of four consecutive
+// words per lane, [chunk][lane][4], so that a lane reads four words with one
+// 128-bit load (the blocks above all start on multiples of four words):
+//   chunk 0-1 W1 (n-tiles 0,1 | 2,3)   chunk 7-8  b1 (n-tiles 0,1 | 2,3)
+//   chunk 2-5 W2 (n-tile 0..3)          chunk 9-10 b2 (n-tiles 0,1 | 2,3)
+//   chunk 6   w3                        chunk 11   b3 (word 0)
+#define MAC_FRAG_CHUNKS 12
+#define MAC_SMEM_FRAG_WORDS (MAC_FRAG_CHUNKS * 4 * 32)
 #define MAC_WALK_WARPS 8
-// the learned walk: below MAC_BAND_LO (group rule) accept, above MAC_BAND_HI open
+// the learned walk's default band: nodes that pass the group rule at
+// MAC_BAND_LO are accepted, nodes that fail it at MAC_BAND_HI opened
 #define MAC_BAND_LO 0.25f
 #define MAC_BAND_HI 1.0f
 
 struct MacDeviceWeights {
     const uint32_t* frag;  // [MAC_FRAG_WORDS][32]: per-lane fragment words (global)
-    uint32_t* smem_frag;   // block copy in shared memory (set by the kernel)
+    const float* band;     // [2]: group-rule theta below which nodes are accepted, above which opened
+    uint32_t* smem_frag;   // block copy in shared memory, chunked (set by the kernel)
     __nv_bfloat16* smem_x; // [warps][x_rows][16] feature tiles (set by the kernel)
     uint32_t x_rows;       // feature rows per warp (32, or more for a queue)
     // recording of training pairs (gbh_mac_generate); rec_count == nullptr: off
@@ -72,6 +82,11 @@ struct GroupGeom {
     float R;           // half diagonal of the group's bounding box
     float a_ref;       // smallest |acceleration| of the group's bodies in the previous step
     float3 bmin, bmax; // the group's bounding box
+    // per-group terms of the features (set by group_feature_terms)
+    float soft;        // softening (length squared)
+    float l_R;         // log2 R
+    float l_soft;      // log2 softening
+    float l_g_aref;    // log2 (G / a_ref); +inf when a_ref == 0
 };
 
 struct NodeGeom {
@@ -80,65 +95,109 @@ struct NodeGeom {
     uint32_t count;
 };
 
-// Distance between the group's box and the node's box (0 when they overlap).
-__device__ __forceinline__ float box_gap(const GroupGeom& g, const NodeGeom& n) {
+// Squared distance between the group's box and the node's box (0 when they
+// overlap).
+__device__ __forceinline__ float box_gap2(const GroupGeom& g, const NodeGeom& n) {
     const float gx = fmaxf(0.0f, fmaxf(n.bmin.x - g.bmax.x, g.bmin.x - n.bmax.x));
     const float gy = fmaxf(0.0f, fmaxf(n.bmin.y - g.bmax.y, g.bmin.y - n.bmax.y));
     const float gz = fmaxf(0.0f, fmaxf(n.bmin.z - g.bmax.z, g.bmin.z - n.bmax.z));
-    return sqrtf(gx * gx + gy * gy + gz * gz);
+    return gx * gx + gy * gy + gz * gz;
 }
 
 // Group theta rule (the learned criterion's ablation): accept when the boxes
 // of the group and the node are disjoint and the node's half side is below
-// theta times the distance from its centre of mass to the group's bounding
-// sphere.
+// theta times the distance D from its centre of mass to the group's bounding
+// sphere, half < theta (D - R), evaluated without a square root as
+// (half + theta R)^2 < theta^2 D^2 (theta > 0).
 __device__ __forceinline__ bool group_theta_accept(const GroupGeom& g, const NodeGeom& n, float theta) {
     const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
     const float half = 0.5f * fmaxf(ex, fmaxf(ey, ez));
     const float dx = n.cm.x - g.cx, dy = n.cm.y - g.cy, dz = n.cm.z - g.cz;
-    const float d = sqrtf(dx * dx + dy * dy + dz * dz) - g.R;
-    return d > 0.0f && half < theta * d && box_gap(g, n) > 0.0f;
+    const float D2 = dx * dx + dy * dy + dz * dz;
+    const float t = half + theta * g.R;
+    return theta > 0.0f && t * t < theta * theta * D2 && box_gap2(g, n) > 0.0f;
+}
+
+// The smallest theta at which the group rule accepts the node,
+// rho = half / (D - R); +inf when the boxes overlap or the centre of mass lies
+// inside the group's bounding sphere.  The learned walk and the recording of
+// training pairs compare it against the band's two thetas.
+__device__ __forceinline__ float group_rho(const GroupGeom& g, const NodeGeom& n) {
+    const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
+    const float half = 0.5f * fmaxf(ex, fmaxf(ey, ez));
+    const float dx = n.cm.x - g.cx, dy = n.cm.y - g.cy, dz = n.cm.z - g.cz;
+    const float den = sqrtf(dx * dx + dy * dy + dz * dz) - g.R;
+    return (den > 0.0f && box_gap2(g, n) > 0.0f) ? __fdividef(half, den) : __int_as_float(0x7f800000);
 }
 
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 
+__device__ __forceinline__ void group_feature_terms(GroupGeom& g, float G, float soft) {
+    g.soft = soft;
+    g.l_R = __log2f(fmaxf(g.R, 1e-30f));
+    g.l_soft = __log2f(soft);  // -inf for zero softening: feature 9 clamps
+    g.l_g_aref = g.a_ref > 0.f ? __log2f(G) - __log2f(g.a_ref) : __int_as_float(0x7f800000);
+}
+
 // The 12 features, all scale free.  h: half of the longest side; d: distance
-// from the node's centre of mass to the group centre; R: group half diagonal.
-__device__ __forceinline__ void mac_features(const GroupGeom& g, const NodeGeom& n, float G, float soft,
-                                             float f[MAC_FEATURES]) {
-    const float tiny = 1e-30f;
+// from the node's centre of mass to the group centre; R: group half diagonal
+// (at least 1e-6 d); off: offset of the centre of mass from the box centre.
+//   f0  log2(h/d)/8            f6  log2(min(count, 2^16))/16
+//   f1  log2(R/d)/8            f7  cos(offset, direction to the group)
+//   f2  log2(1 - R/d)/8        f8  log2(G m / (d^2 + soft) / a_ref)/16
+//   f3  off/h                  f9  log2(soft / d^2)/16
+//   f4  shortest/longest side  f10 log2(h/R)/8
+//   f5  middle/longest side    f11 log2(max(box gap, 1e-6 h)/h)/8
+// They are inputs of a BF16 network (8 significant bits), so the fast
+// hardware log2, reciprocal and reciprocal square root are accurate enough;
+// the logarithms of group terms are computed once per group.
+__device__ __forceinline__ void mac_features(const GroupGeom& g, const NodeGeom& n, float f[MAC_FEATURES]) {
     const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
     const float emax = fmaxf(ex, fmaxf(ey, ez));
     const float emin = fminf(ex, fminf(ey, ez));
     const float emid = ex + ey + ez - emax - emin;
-    const float h = fmaxf(0.5f * emax, tiny);
+    const float h = fmaxf(0.5f * emax, 1e-30f);
     const float dx = n.cm.x - g.cx, dy = n.cm.y - g.cy, dz = n.cm.z - g.cz;
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    const float d = fmaxf(sqrtf(d2), tiny);
-    const float R = fmaxf(g.R, 1e-6f * d);
-    const float q = clampf((d - R) / d, 1e-4f, 1.0f);
+    const float d2 = fmaxf(dx * dx + dy * dy + dz * dz, 1e-36f);
+    const float inv_d = rsqrtf(d2);
+    const float l_d2 = __log2f(d2);
+    const float l_d = 0.5f * l_d2;
+    const float l_h = __log2f(h);
+    const float l_R = fmaxf(g.l_R, l_d - 19.931568f);  // R >= 1e-6 d
+    const float R = fmaxf(g.R, 1e-6f * d2 * inv_d);
+    const float inv_h = __fdividef(1.0f, h);
     const float ox = n.cm.x - 0.5f * (n.bmin.x + n.bmax.x);
     const float oy = n.cm.y - 0.5f * (n.bmin.y + n.bmax.y);
     const float oz = n.cm.z - 0.5f * (n.bmin.z + n.bmax.z);
-    const float off = sqrtf(ox * ox + oy * oy + oz * oz);
-    const float force = G * n.cm.w / (d2 + soft);
-    f[0] = clampf(__log2f(h / d), -24.f, 8.f) * 0.125f;
-    f[1] = clampf(__log2f(R / d), -24.f, 8.f) * 0.125f;
-    f[2] = __log2f(q) * 0.125f;
-    f[3] = clampf(off / h, 0.f, 2.f);
-    f[4] = emax > 0.f ? emin / emax : 1.f;
-    f[5] = emax > 0.f ? emid / emax : 1.f;
-    f[6] = __log2f((float)min(n.count, 1u << 16)) * (1.0f / 16.0f);
-    f[7] = off > tiny ? (ox * dx + oy * dy + oz * dz) / (off * d) : 0.f;
-    f[8] = (g.a_ref > 0.f ? clampf(__log2f(force / g.a_ref), -32.f, 32.f) : 32.f) * (1.0f / 16.0f);
-    f[9] = clampf(__log2f(soft / d2 + 1e-30f), -48.f, 8.f) * (1.0f / 16.0f);
-    f[10] = clampf(__log2f(h / R), -16.f, 16.f) * 0.125f;
-    f[11] = clampf(__log2f(box_gap(g, n) / h + 1e-6f), -20.f, 8.f) * 0.125f;
+    const float off2 = ox * ox + oy * oy + oz * oz;
+    const float inv_off = rsqrtf(fmaxf(off2, 1e-36f));
+    const float inv_emax = emax > 0.f ? __fdividef(1.0f, emax) : 0.f;
+    const float gap2 = box_gap2(g, n);
+    f[0] = clampf(l_h - l_d, -24.f, 8.f) * 0.125f;
+    f[1] = clampf(l_R - l_d, -24.f, 8.f) * 0.125f;
+    f[2] = __log2f(clampf(1.0f - R * inv_d, 1e-4f, 1.0f)) * 0.125f;
+    f[3] = clampf(off2 * inv_off * inv_h, 0.f, 2.f);
+    f[4] = emax > 0.f ? emin * inv_emax : 1.f;
+    f[5] = emax > 0.f ? emid * inv_emax : 1.f;
+    f[6] = __log2f((float)min(max(n.count, 1u), 1u << 16)) * (1.0f / 16.0f);
+    f[7] = off2 > 1e-36f ? clampf((ox * dx + oy * dy + oz * dz) * inv_off * inv_d, -1.f, 1.f) : 0.f;
+    f[8] = clampf(g.l_g_aref + __log2f(n.cm.w) - __log2f(d2 + g.soft), -32.f, 32.f) * (1.0f / 16.0f);
+    f[9] = clampf(g.l_soft - l_d2, -48.f, 8.f) * (1.0f / 16.0f);
+    f[10] = clampf(l_h - l_R, -16.f, 16.f) * 0.125f;
+    f[11] = clampf(0.5f * __log2f(fmaxf(gap2, 1e-12f * h * h)) - l_h, -20.f, 8.f) * 0.125f;
 }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// ReLU and BF16 rounding of two values in one instruction (the same result as
+// rounding max(x, 0): rounding keeps the sign)
+__device__ __forceinline__ uint32_t pack_bf16x2_relu(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
 }
 
 __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
@@ -167,14 +226,18 @@ struct MacActs {
 };
 
 // Forward pass of the warp's 32 staged rows; returns row `lane`'s output.
+// The two 16-row m-tiles go through all three layers one after the other,
+// which keeps the live accumulators to one tile's.  KEEP also returns the
+// FP32 activations (training); inference fuses ReLU into the BF16 packing.
 template <bool KEEP>
 __device__ __forceinline__ float mac_forward_warp(const MacDeviceWeights& mw, uint32_t warp, uint32_t lane,
                                                   MacActs* acts) {
     __syncwarp();
     const uint32_t gid = lane >> 2, tig = lane & 3;
-    const uint32_t* F = mw.smem_frag;
+    const uint4* F4 = reinterpret_cast<const uint4*>(mw.smem_frag) + lane;  // chunk c at F4[32 c]
     const uint32_t* X = reinterpret_cast<const uint32_t*>(mw.smem_x + (size_t)warp * mw.x_rows * 16);
-    uint32_t a2[2][2][4];  // layer-2 A fragments [m-tile][k-step]
+    auto act = [&](float x0, float x1) { return KEEP ? pack_bf16x2(x0, x1) : pack_bf16x2_relu(x0, x1); };
+    float out[2][2];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
         uint32_t a[4];
@@ -182,66 +245,60 @@ __device__ __forceinline__ float mac_forward_warp(const MacDeviceWeights& mw, ui
         a[1] = X[(16 * mt + gid + 8) * 8 + tig];
         a[2] = X[(16 * mt + gid) * 8 + tig + 4];
         a[3] = X[(16 * mt + gid + 8) * 8 + tig + 4];
-        float c[4][4];
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const float b0 = __uint_as_float(F[(MAC_FRAG_W1 + MAC_FRAG_W2 + MAC_FRAG_W3 + 2 * nt) * 32 + lane]);
-            const float b1 = __uint_as_float(F[(MAC_FRAG_W1 + MAC_FRAG_W2 + MAC_FRAG_W3 + 2 * nt + 1) * 32 + lane]);
-            c[nt][0] = b0;
-            c[nt][1] = b1;
-            c[nt][2] = b0;
-            c[nt][3] = b1;
-            mma_bf16(c[nt], a, F[(2 * nt) * 32 + lane], F[(2 * nt + 1) * 32 + lane]);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) c[nt][r] = fmaxf(c[nt][r], 0.0f);
-            if (KEEP)
-#pragma unroll
-                for (int r = 0; r < 4; ++r) acts->h1[mt][nt][r] = c[nt][r];
-        }
+        // layer 1: 16 x 12(16) by 12(16) x 32, ReLU; n-tiles 2 ks, 2 ks + 1
+        uint32_t a2[2][4];  // layer-2 A fragments [k-step]
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks) {
-            a2[mt][ks][0] = pack_bf16x2(c[2 * ks][0], c[2 * ks][1]);
-            a2[mt][ks][1] = pack_bf16x2(c[2 * ks][2], c[2 * ks][3]);
-            a2[mt][ks][2] = pack_bf16x2(c[2 * ks + 1][0], c[2 * ks + 1][1]);
-            a2[mt][ks][3] = pack_bf16x2(c[2 * ks + 1][2], c[2 * ks + 1][3]);
+            const uint4 wv = F4[32 * ks];
+            const uint4 bv = F4[32 * (7 + ks)];
+            float c[2][4] = {{__uint_as_float(bv.x), __uint_as_float(bv.y), __uint_as_float(bv.x), __uint_as_float(bv.y)},
+                             {__uint_as_float(bv.z), __uint_as_float(bv.w), __uint_as_float(bv.z), __uint_as_float(bv.w)}};
+            mma_bf16(c[0], a, wv.x, wv.y);
+            mma_bf16(c[1], a, wv.z, wv.w);
+            if (KEEP) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        c[h][r] = fmaxf(c[h][r], 0.0f);
+                        acts->h1[mt][2 * ks + h][r] = c[h][r];
+                    }
+            }
+            a2[ks][0] = act(c[0][0], c[0][1]);
+            a2[ks][1] = act(c[0][2], c[0][3]);
+            a2[ks][2] = act(c[1][0], c[1][1]);
+            a2[ks][3] = act(c[1][2], c[1][3]);
         }
-    }
-    float out[2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-        float c[4][4];
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const int bo = MAC_FRAG_W1 + MAC_FRAG_W2 + MAC_FRAG_W3 + MAC_FRAG_B1;
-            const float b0 = __uint_as_float(F[(bo + 2 * nt) * 32 + lane]);
-            const float b1 = __uint_as_float(F[(bo + 2 * nt + 1) * 32 + lane]);
-            c[nt][0] = b0;
-            c[nt][1] = b1;
-            c[nt][2] = b0;
-            c[nt][3] = b1;
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks)
-                mma_bf16(c[nt], a2[mt][ks], F[(MAC_FRAG_W1 + (nt * 2 + ks) * 2) * 32 + lane],
-                         F[(MAC_FRAG_W1 + (nt * 2 + ks) * 2 + 1) * 32 + lane]);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) c[nt][r] = fmaxf(c[nt][r], 0.0f);
-            if (KEEP)
-#pragma unroll
-                for (int r = 0; r < 4; ++r) acts->h2[mt][nt][r] = c[nt][r];
-        }
+        // layer 2: 16 x 32 by 32 x 32, ReLU; its output is layer 3's A
         uint32_t a3[2][4];
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks) {
-            a3[ks][0] = pack_bf16x2(c[2 * ks][0], c[2 * ks][1]);
-            a3[ks][1] = pack_bf16x2(c[2 * ks][2], c[2 * ks][3]);
-            a3[ks][2] = pack_bf16x2(c[2 * ks + 1][0], c[2 * ks + 1][1]);
-            a3[ks][3] = pack_bf16x2(c[2 * ks + 1][2], c[2 * ks + 1][3]);
-        }
-        float o[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int ks3 = 0; ks3 < 2; ++ks3) {
+            const uint4 bv = F4[32 * (9 + ks3)];
+            float c[2][4] = {{__uint_as_float(bv.x), __uint_as_float(bv.y), __uint_as_float(bv.x), __uint_as_float(bv.y)},
+                             {__uint_as_float(bv.z), __uint_as_float(bv.w), __uint_as_float(bv.z), __uint_as_float(bv.w)}};
 #pragma unroll
-        for (int ks = 0; ks < 2; ++ks)
-            mma_bf16(o, a3[ks], F[(MAC_FRAG_W1 + MAC_FRAG_W2 + 2 * ks) * 32 + lane],
-                     F[(MAC_FRAG_W1 + MAC_FRAG_W2 + 2 * ks + 1) * 32 + lane]);
+            for (int h = 0; h < 2; ++h) {
+                const int nt = 2 * ks3 + h;
+                const uint4 wv = F4[32 * (2 + nt)];  // (k-step 0: b0 b1, k-step 1: b0 b1)
+                mma_bf16(c[h], a2[0], wv.x, wv.y);
+                mma_bf16(c[h], a2[1], wv.z, wv.w);
+                if (KEEP)
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        c[h][r] = fmaxf(c[h][r], 0.0f);
+                        acts->h2[mt][nt][r] = c[h][r];
+                    }
+            }
+            a3[ks3][0] = act(c[0][0], c[0][1]);
+            a3[ks3][1] = act(c[0][2], c[0][3]);
+            a3[ks3][2] = act(c[1][0], c[1][1]);
+            a3[ks3][3] = act(c[1][2], c[1][3]);
+        }
+        // layer 3: 16 x 32 by 32 x 1 (one useful column of an n8 tile)
+        const uint4 w3 = F4[32 * 6];
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_bf16(o, a3[0], w3.x, w3.y);
+        mma_bf16(o, a3[1], w3.z, w3.w);
         out[mt][0] = o[0];  // row 16 mt + gid, column 0 (valid in lanes with tig == 0)
         out[mt][1] = o[2];  // row 16 mt + gid + 8
     }
@@ -253,7 +310,7 @@ __device__ __forceinline__ float mac_forward_warp(const MacDeviceWeights& mw, ui
     const float v11 = __shfl_sync(0xffffffffu, out[1][1], src);
     const uint32_t sel = lane >> 3;
     const float v = sel == 0 ? v00 : sel == 1 ? v01 : sel == 2 ? v10 : v11;
-    const float b3 = __uint_as_float(F[(MAC_FRAG_WORDS - 1) * 32 + lane]);
+    const float b3 = __uint_as_float(mw.smem_frag[(11 * 32 + lane) * 4]);
     return v + b3;
 }
 
@@ -261,10 +318,15 @@ __device__ __forceinline__ float mac_infer_warp(const MacDeviceWeights& mw, uint
     return mac_forward_warp<false>(mw, warp, lane, nullptr);
 }
 
-// Copy the fragment table into the block's shared memory (all threads).
+// Copy the fragment table into the block's shared memory (all threads);
+// smem_frag holds MAC_SMEM_FRAG_WORDS words.
 __device__ __forceinline__ void mac_load_frag(MacDeviceWeights& mw, uint32_t* smem_frag, __nv_bfloat16* smem_x,
                                               uint32_t x_rows = 32) {
-    for (uint32_t i = threadIdx.x; i < MAC_FRAG_WORDS * 32; i += blockDim.x) smem_frag[i] = mw.frag[i];
+    // [word][lane] in global memory -> [chunk][lane][4] here
+    for (uint32_t i = threadIdx.x; i < MAC_FRAG_WORDS * 32; i += blockDim.x) {
+        const uint32_t word = i >> 5, l = i & 31;
+        smem_frag[((word >> 2) * 32 + l) * 4 + (word & 3)] = mw.frag[i];
+    }
     mw.smem_frag = smem_frag;
     mw.smem_x = smem_x;
     mw.x_rows = x_rows;

@@ -283,6 +283,13 @@ int gbh_direct_sum(gbh_ctx* ctx, const gbh_step_params* params, const uint32_t* 
 #define GBH_MAC_NUM_PARAMS (32 * 12 + 32 + 32 * 32 + 32 + 32 + 1)
 int gbh_mac_set_weights(gbh_ctx* ctx, const float* params, uint32_t count);
 int gbh_mac_get_weights(gbh_ctx* ctx, float* params, uint32_t count);
+/* The band the network decides, as two group-rule thetas (half side of the
+ * node < theta x distance from its centre of mass to the group's bounding
+ * sphere): nodes that pass the rule at theta_accept are accepted without the
+ * network, nodes that fail it at theta_open are opened without it.  Defaults
+ * 0.25 and 1.0.  Training pairs are recorded in the same band. */
+int gbh_mac_set_band(gbh_ctx* ctx, float theta_accept, float theta_open);
+int gbh_mac_get_band(gbh_ctx* ctx, float* theta_accept, float* theta_open);
 /* Sample (32-body group, node) pairs from the current tree, compute their
  * features and labels (log10 of the relative error of accepting the node's
  * monopole against its exact subtree sum, max over the group) into device
