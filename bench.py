@@ -1,15 +1,24 @@
-"""Benchmark of the GB300 Barnes–Hut step: steps/s at 16.7M bodies.
+"""Benchmark of the GB300 Barnes–Hut step: steps/s at 16.7M bodies, the
+learned acceptance criterion against the plain theta = 0.5 walk at equal p99
+acceleration error.
 
 Workload (default): 16,777,216 bodies, 70% Plummer (a=1) + 30% uniform in
-[-3,3]^3, equal masses, G=1, eps=0.005 (softening = eps^2), theta=0.5,
-dt=1e-3, dynamic bounds, no merges; seeded synthetic input (seed 3).
+[-3,3]^3, equal masses, G=1, eps=0.005 (softening = eps^2), dt=1e-3, dynamic
+bounds, no merges; seeded synthetic input (seed 3).
+
+Before timing (untimed): the MLP is trained on this state on the GPU
+(gbh_mac_generate + gbh_mac_train), the direct-sum judge takes 4096 sampled
+bodies, and the learned walk's tolerance is the one with the fewest
+interactions whose p99 error is at or below the plain theta = 0.5 walk's.
 
 One step = BarnesHut.step of the reference: compaction, AABB + Morton encode,
 radix sort, LBVH build, bottom-up fill, tree walk + update, merge, swap,
 launched as one CUDA graph.  The timed region holds exactly K steps between
 CUDA events recorded on the context stream, with a barrier and a device
 synchronise on both sides.  The inputs (16.7M bodies, 537 MB of bodies plus
-~5 GB of tree and sort buffers) are far larger than the 129 MB L2.
+~5 GB of tree and sort buffers) are far larger than the 129 MB L2.  The plain
+theta = 0.5 walk and the group-theta ablation are then timed the same way on
+the same context ("comparison").
 
 Output: one JSON line (rank 0).  `--impl reference` times the reference
 algorithm on the host CPU cores (the C restatement under oracle/, since the
@@ -274,55 +283,157 @@ def run_reference(args):
     return 0
 
 
+LEARNED_TAUS = [-3.0, -2.75, -2.5, -2.25, -2.0, -1.75, -1.5]
+GROUP_THETAS = [0.4, 0.45, 0.5, 0.55, 0.6, 0.65, 0.7]
+PLAIN_THETAS = [0.3, 0.5, 0.7]
+# DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture
+# (profiles/walk_learned_mixture4M.md), divided by its bodies; the walk's
+# traffic grows in proportion to the bodies
+WALK_LEARNED_DRAM_BYTES_PER_BODY = None
+
+
+def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
+    """W untimed steps, then exactly K steps between CUDA events on the
+    context stream, barrier + device synchronise on both sides; max over ranks."""
+    import torch
+
+    for _ in range(warmup):
+        bh.step(p)
+    bh.synchronize()
+    barrier(dist, local)
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    bh.step(p, count=steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier(dist, local)
+    clk = clocks.stop() if clocks else None
+    ms = max_over_ranks(dist, ev0.elapsed_time(ev1), local)
+    st = bh.read_stats()
+    return ms, st, clk
+
+
+def kernels_per_step(mac_mode: int) -> int:
+    """Kernels of this library launched by one step (the CUDA graph's kernel
+    nodes): reset 1, prepare 3, sort 1 + 8 passes, build 1, fill 2, walk 1
+    (+ group finding 1 for the group and learned walks), merge resolution 4
+    (they exit at once without merge tasks), swap 0 (a pointer swap)."""
+    return 1 + 3 + 9 + 1 + 2 + 1 + 4 + (1 if mac_mode != abi.MAC_PLAIN else 0)
+
+
 def run_ours(args):
     import torch
 
     dist, rank, world, local = dist_setup()
     torch.cuda.set_device(local)
-    from gravity_gb300 import BarnesHut
+    from gravity_gb300 import BarnesHut, accuracy
 
     wl = workload(args.workload, args.n)
     bodies = wl["bodies"]()
     bounds = wl.get("bounds", ic.exact_bounds(bodies))
     units = abi.units(G=1.0)
-    p = wl["params"]
+    p_plain = wl["params"]
+    merging = p_plain.merging_collision_or_neither != abi.MODE_NEITHER
     bh = BarnesHut(wl["n"], bounds, units, device=local)
     bh.upload_bodies(bodies)
     bh.init()
     stream = torch.cuda.ExternalStream(bh.stream, device=f"cuda:{local}")
-    for _ in range(args.warmup):
-        bh.step(p)
-    bh.synchronize()
-    st = bh.read_stats()
-    interactions = int(st.interactions)
+    soft = p_plain.softening
 
+    def learned(t):
+        return abi.step_params(dt=p_plain.dt, theta=p_plain.theta, softening=soft, bounds=p_plain.static_or_dynamic,
+                               mac=abi.MAC_LEARNED, mac_tolerance=t)
+
+    def group(t):
+        return abi.step_params(dt=p_plain.dt, theta=t, softening=soft, bounds=p_plain.static_or_dynamic,
+                               mac=abi.MAC_GROUP)
+
+    def plain(t):
+        return abi.step_params(dt=p_plain.dt, theta=t, softening=soft, bounds=p_plain.static_or_dynamic)
+
+    # ---- learned criterion: train on this state, then pick the tolerance whose
+    # p99 error stays at or below the plain theta = 0.5 walk's (untimed)
+    calib = {}
+    p_head = p_plain
+    mac_name = "plain"
+    if not merging and not args.plain_only:
+        t0 = time.perf_counter()
+        if args.mac_weights:
+            bh.mac_set_weights(np.load(args.mac_weights))
+            calib["weights"] = os.path.basename(args.mac_weights)
+        else:
+            pairs = bh.mac_generate(p_plain, max_pairs=args.mac_pairs, seed=1)
+            losses = bh.mac_train(epochs=args.mac_epochs, batch=16384, lr=3e-3, seed=0)
+            calib["training"] = {"pairs": pairs, "epochs": args.mac_epochs, "loss_first": float(losses[0]),
+                                 "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
+        judge = accuracy.Judge(bh, p_plain, count=4096, seed=2)
+        ref = {th: accuracy.evaluate(bh, judge, plain(th)) for th in PLAIN_THETAS}
+        target = ref[p_plain.theta]["p99"] if p_plain.theta in ref else accuracy.evaluate(bh, judge, p_plain)["p99"]
+        calib["plain"] = {str(th): {k: r[k] for k in ("median", "p90", "p99", "max", "interactions")}
+                          for th, r in ref.items()}
+        calib["p99_target"] = target
+        if args.mac_tolerance is not None:
+            tau = args.mac_tolerance
+            r = accuracy.evaluate(bh, judge, learned(tau))
+            best_l = (tau, r)
+        else:
+            best_l, res_l = accuracy.match_p99(bh, judge, learned, LEARNED_TAUS, target)
+            calib["learned_sweep"] = [{k: r[k] for k in ("setting", "p99", "interactions", "mac_evaluations")}
+                                      for r in res_l]
+        if best_l is None:
+            raise SystemExit("no learned tolerance reaches the plain walk's p99 error")
+        calib["learned"] = {k: best_l[1][k] for k in ("median", "p90", "p99", "max", "interactions",
+                                                        "mac_evaluations")}
+        calib["learned"]["mac_tolerance"] = best_l[0]
+        p_head = learned(best_l[0])
+        mac_name = "learned"
+        if not args.no_compare:
+            best_g, res_g = accuracy.match_p99(bh, judge, group, GROUP_THETAS, target)
+            if best_g is not None:
+                calib["group"] = {k: best_g[1][k] for k in ("median", "p90", "p99", "max", "interactions")}
+                calib["group"]["theta"] = best_g[0]
+        calib["band"] = list(bh.mac_get_band())
+
+    # ---- headline: K timed steps of the chosen walk
     clocks = ClockSampler(local)
-    barrier(dist, local)
-    torch.cuda.synchronize()
-    clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    bh.step(p, count=args.steps)
-    ev1.record(stream)
-    ev1.synchronize()
-    torch.cuda.synchronize()
-    barrier(dist, local)
-    clk = clocks.stop()
-    ms_total = ev0.elapsed_time(ev1)
-    ms_total = max_over_ranks(dist, ms_total, local)
+    ms_total, st, clk = timed_steps(bh, p_head, args.steps, args.warmup, stream, dist, local, clocks)
     ms_step = ms_total / args.steps
     value = world * args.steps / (ms_total / 1000.0)
-    bh.synchronize()
-    st = bh.read_stats()
+    interactions = int(st.interactions)
 
-    # per-stage times (CUDA events between eager stage launches on the context stream)
-    prof = [bh.step_profiled(p) for _ in range(3)]
+    # per-stage times of the chosen walk (CUDA events between eager stage launches)
+    prof = [bh.step_profiled(p_head) for _ in range(3)]
     stage_ms = {k: float(np.median([d[k] for d in prof])) for k in abi.STAGE_NAMES}
     st_prof = bh.read_stats()
-    walk_ms = stage_ms["walk"]
-    walk_flop = WALK_FLOP_PER_INTERACTION * int(st_prof.interactions)
-    fp32_peak = None
+
+    # ---- comparison arms on the same context, same timing rules
+    compare = {}
+    if mac_name == "learned" and not args.no_compare:
+        ms_p, st_p, clk_p = timed_steps(bh, p_plain, args.steps, args.warmup, stream, dist, local,
+                                        ClockSampler(local))
+        compare["plain_theta"] = {"theta": p_plain.theta, "steps_per_s": world * args.steps / (ms_p / 1000.0),
+                                  "ms_per_step": ms_p / args.steps, "p99": calib["plain"][str(p_plain.theta)]["p99"],
+                                  "interactions_per_step": int(st_p.interactions), "clocks": clk_p}
+        compare["learned"] = {"mac_tolerance": calib["learned"]["mac_tolerance"], "steps_per_s": value,
+                              "ms_per_step": ms_step, "p99": calib["learned"]["p99"],
+                              "interactions_per_step": interactions,
+                              "mac_evaluations_per_step": int(st.mac_evaluations)}
+        compare["learned_speedup_vs_plain"] = value / compare["plain_theta"]["steps_per_s"]
+        if "group" in calib:
+            ms_g, st_g, _ = timed_steps(bh, group(calib["group"]["theta"]), args.steps, args.warmup, stream, dist,
+                                        local)
+            compare["group_theta_ablation"] = {"theta": calib["group"]["theta"],
+                                               "steps_per_s": world * args.steps / (ms_g / 1000.0),
+                                               "ms_per_step": ms_g / args.steps, "p99": calib["group"]["p99"],
+                                               "interactions_per_step": int(st_g.interactions)}
+
+    # ---- roofline of the dominant kernel (the walk)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -330,33 +441,44 @@ def run_ours(args):
     except (OSError, ValueError):
         peaks = {}
     sm_max = peaks.get("sm_max_mhz", 2070.0)
-    # FP32 FMA pipe: 152 SMs x 128 lanes x 2 flop x max SM clock
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FP32 FMA lanes x 2 flop x max SM clock
+    walk_ms = stage_ms["walk"]
+    walk_flop = WALK_FLOP_PER_INTERACTION * int(st_prof.interactions)
+    mlp_flop = 2 * (12 * 32 + 32 * 32 + 32) * int(st_prof.mac_evaluations)
     achieved = walk_flop / (walk_ms / 1000.0) / 1e12
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     n_live = int(st_prof.alive)
     sort_bytes = (8 + 24 * 8) * n_live
     sort_gbs = sort_bytes / (stage_ms["sort"] / 1000.0) / 1e9
+    traffic = None
+    if mac_name == "learned" and WALK_LEARNED_DRAM_BYTES_PER_BODY:
+        traffic = WALK_LEARNED_DRAM_BYTES_PER_BODY * n_live
 
-    # e2e through the public API with host buffers: per step the parameters go
-    # host->device and the live positions + SimulationValues come back
-    pos_host = np.empty(wl["n"], dtype=abi.BODY_DTYPE)
+    # ---- e2e through the public API with host buffers: per step the bodies go
+    # host->device from pinned memory, one step runs, and the bodies come back
+    n = wl["n"]
+    pin_in = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
+    pin_out = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
+    bh.read_bodies(out=pin_in)
     e2e_steps = max(3, min(args.steps, 10))
+    bh.step(p_head)  # warm the graph of this parity
+    bh.read_bodies(out=pin_in)
     barrier(dist, local)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        bh.step(p)
-        pos_host[:] = bh.read_bodies()
-        bh.read_sim_values()
+        bh.upload_bodies(pin_in)
+        bh.step(p_head)
+        bh.read_bodies(out=pin_out)
     t1 = time.perf_counter()
-    e2e_val = max_over_ranks(dist, (t1 - t0), local)
+    e2e_s = max_over_ranks(dist, t1 - t0, local)
     e2e = {
-        "value": world * e2e_steps / e2e_val,
+        "value": world * e2e_steps / e2e_s,
         "unit": "steps/s",
-        "h2d_bytes_per_step": C.sizeof(abi.StepParams),
-        "d2h_bytes_per_step": wl["n"] * abi.BODY_DTYPE.itemsize + C.sizeof(abi.SimValues),
+        "h2d_bytes_per_step": n * abi.BODY_DTYPE.itemsize + C.sizeof(abi.StepParams),
+        "d2h_bytes_per_step": n * abi.BODY_DTYPE.itemsize,
+        "path": "BarnesHut.upload_bodies + step + read_bodies (C-ABI gbh_upload_bodies / gbh_step / "
+                "gbh_read_bodies), pinned host buffers",
     }
-    launches_per_step = 1 + 3 + 1 + 8 + 1 + 1 + 1 + 4  # reset, prepare x3, sort scan + 8 passes, build, fill, walk, merge x4
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, bodies, bounds, units, budget_s=args.cpu_budget)
@@ -378,26 +500,30 @@ def run_ours(args):
         "config": {
             "workload": wl["name"],
             "n_bodies": wl["n"],
-            "theta": p.theta,
-            "softening": p.softening,
-            "mac": "plain",
+            "softening": soft,
+            "mac": mac_name,
+            "mac_tolerance": calib.get("learned", {}).get("mac_tolerance"),
+            "plain_theta": p_plain.theta,
             "l2": "inputs larger than L2 (bodies 537 MB, tree + sort buffers ~5 GB)",
             "parallelism": f"replicas x{world}",
         },
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": kernels_per_step(p_head.mac_mode) * args.steps,
         "interactions_per_step": interactions,
         "interactions_per_s": interactions * value / world,
+        "comparison": compare,
+        "calibration": calib,
         "stage_ms": stage_ms,
         "roofline": {
-            "kernel": "k_walk_plain",
+            "kernel": "k_walk_group<learned>" if mac_name == "learned" else "k_walk_plain",
             "bound": "fp32",
             "achieved": achieved,
             "peak": fp32_peak,
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "traffic": None,
-            "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json",
+            "traffic": traffic,
+            "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json (of measured clock)",
             "flop_per_interaction": WALK_FLOP_PER_INTERACTION,
+            "mlp_tflops": mlp_flop / (walk_ms / 1000.0) / 1e12,
         },
         "roofline_sort": {
             "kernel": "k_sort_pass x8 + k_sort_scan",
@@ -413,7 +539,6 @@ def run_ours(args):
         "e2e": e2e,
         "clocks": clk,
         "stats": abi.stats_to_dict(st),
-        "footprint_bytes": None,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -430,6 +555,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-stride", type=int, default=256)
+    ap.add_argument("--plain-only", action="store_true", help="time the plain theta walk only")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain and group-theta comparison arms")
+    ap.add_argument("--mac-weights", default=None, help="load MLP weights (.npy) instead of training")
+    ap.add_argument("--mac-tolerance", type=float, default=None, help="fixed tolerance instead of calibration")
+    ap.add_argument("--mac-pairs", type=int, default=8_000_000)
+    ap.add_argument("--mac-epochs", type=int, default=12)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -127,9 +127,14 @@ class BarnesHut:
         return dict(zip(abi.STAGE_NAMES, [float(x) for x in ms]))
 
     # ---- read-back -----------------------------------------------------------
-    def read_bodies(self, which=abi.BODIES_IN, count=None, offset=0) -> np.ndarray:
+    def read_bodies(self, which=abi.BODIES_IN, count=None, offset=0, out: np.ndarray | None = None) -> np.ndarray:
+        """Bodies [offset, offset + count) of the input (or output) buffer,
+        into `out` when given (a contiguous BODY_DTYPE array, e.g. pinned)."""
         count = self.n - offset if count is None else count
-        out = np.zeros(count, dtype=abi.BODY_DTYPE)
+        if out is None:
+            out = np.zeros(count, dtype=abi.BODY_DTYPE)
+        elif out.dtype != abi.BODY_DTYPE or len(out) < count or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous BODY_DTYPE array of at least count bodies")
         self._chk(lib().gbh_read_bodies(self._h, which, _ptr(out), count, offset))
         return out
 

@@ -61,6 +61,7 @@ struct DevState {
     uint32_t sort_tiles[SORT_PASSES];  // onesweep tile tickets
     uint32_t num_groups;               // body groups of the group walk
     uint32_t frontier_saturated;       // group walks that accepted instead of opening (full stack)
+    uint32_t fill_frontier;            // nodes handed from the tiled fill to the top-tree fill
     unsigned long long interactions;
     unsigned long long opened;
     unsigned long long mac_evals;
@@ -99,6 +100,8 @@ struct StepBuffers {
     float* accel_mag;     // |acceleration| of the last walk, by body id (learned MAC feature)
     uint32_t* node_lo;    // first sorted slot of each internal node's leaf range
     uint2* groups;        // (first slot, body count) of the group walk's body groups
+    uint2* fill_frontier; // (node, bodies) handed from the tiled fill to the top-tree fill
+    uint32_t fill_frontier_cap;
     // compaction scratch
     uint32_t* tile_dead;
     float* tile_aabb;

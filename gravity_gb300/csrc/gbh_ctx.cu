@@ -75,6 +75,10 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.accel_mag = c->accel_mag;
     b.node_lo = c->node_lo;
     b.groups = c->groups;
+    // the fill's frontier lives in the sort's spare key buffer (free once the
+    // sorted keys are back in keys_in, until the next step's encode)
+    b.fill_frontier = reinterpret_cast<uint2*>(c->keys[1 - c->iin]);
+    b.fill_frontier_cap = c->N;
     b.tile_dead = c->tile_dead;
     b.tile_aabb = c->tile_aabb;
     b.hist = c->hist;
@@ -259,6 +263,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
 
     sort_setup();
     group_walk_setup();
+    fill_setup();
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->arena, 0, A.total, c->stream);
     // SimulationValues as packed by GPU.packValues (GPU.java:1096-1143)

@@ -64,3 +64,4 @@ int enqueue_walk_learned(gbh_ctx* c);
 void mac_release(gbh_ctx* c);
 void sort_setup();
 void group_walk_setup();
+void fill_setup();

@@ -39,6 +39,7 @@ __global__ void k_reset(StepBuffers b) {
         st->opened = 0;
         st->mac_evals = 0;
         st->frontier_saturated = 0;
+        st->fill_frontier = 0;
         // units update, bh_update.comp:22-25 / common.glsl:346-360
         if (p->units.mass != 0.0f) {
             gbh_sim_values* sim = b.sim;

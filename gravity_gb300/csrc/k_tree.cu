@@ -154,44 +154,223 @@ __device__ __forceinline__ WalkRec make_rec(const NodeVals& v, uint32_t id, uint
     return r;
 }
 
-__global__ __launch_bounds__(256) void k_fill(StepBuffers b) {
+// One internal node from its two children (bh_tree.comp:223-246); L is
+// childA's values, R childB's.
+__device__ __forceinline__ NodeVals combine(const NodeVals& L, const NodeVals& R) {
+    const float lw = L.cm.w, rw = R.cm.w;
+    const float M = lw + rw;
+    NodeVals out;
+    if (M > 0.0f) {
+        out.cm.x = (lw * L.cm.x + rw * R.cm.x) / M;
+        out.cm.y = (lw * L.cm.y + rw * R.cm.y) / M;
+        out.cm.z = (lw * L.cm.z + rw * R.cm.z) / M;
+        out.col.x = (lw * L.col.x + rw * R.col.x) / M;
+        out.col.y = (lw * L.col.y + rw * R.col.y) / M;
+        out.col.z = (lw * L.col.z + rw * R.col.z) / M;
+    } else {
+        out.cm.x = (L.cm.x + R.cm.x) * 0.5f;
+        out.cm.y = (L.cm.y + R.cm.y) * 0.5f;
+        out.cm.z = (L.cm.z + R.cm.z) * 0.5f;
+        out.col.x = (L.col.x + R.col.x) * 0.5f;
+        out.col.y = (L.col.y + R.col.y) * 0.5f;
+        out.col.z = (L.col.z + R.col.z) * 0.5f;
+    }
+    out.cm.w = M;
+    out.col.w = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        out.box[k] = gmin(L.box[k], R.box[k]);
+        out.box[3 + k] = gmax(L.box[3 + k], R.box[3 + k]);
+    }
+    out.depth = 1u + max(L.depth, R.depth);
+    return out;
+}
+
+// Write a finished internal node: its Node words (reference layout), the
+// walk records of its two children, and mark it claimed (readyChildren =
+// 0xFFFFFFFF, bh_tree.comp:200).
+__device__ __forceinline__ void store_internal(const StepBuffers& b, uint32_t i, const NodeVals& out, const NodeVals& L,
+                                               const NodeVals& R, uint32_t a_id, uint32_t b_id, uint32_t a_count,
+                                               uint32_t b_count) {
+    gbh_node* nd = &b.internal[i];
+    float4* np = reinterpret_cast<float4*>(nd);
+    __stcg(np + 0, out.cm);
+    __stcg(np + 1, make_float4(out.box[0], out.box[1], out.box[2], out.box[3]));
+    __stcg(reinterpret_cast<float2*>(np + 2), make_float2(out.box[4], out.box[5]));
+    nd->node_depth = out.depth;
+    nd->ready_children = GBH_NONE;
+    __stcg(np + 4, out.col);
+    ChildPair pr;
+    pr.a = make_rec(L, a_id, a_count, a_id < b.N);
+    pr.b = make_rec(R, b_id, b_count, b_id < b.N);
+    b.pairs[i] = pr;
+}
+
+// Node values kept in shared memory by the tiled fill (64 bytes)
+struct TileVals {
+    float4 cm;
+    float4 col;
+    float4 box03;
+    float box4, box5;
+    uint32_t depth, pad;
+};
+
+__device__ __forceinline__ TileVals to_tile(const NodeVals& v) {
+    TileVals t;
+    t.cm = v.cm;
+    t.col = v.col;
+    t.box03 = make_float4(v.box[0], v.box[1], v.box[2], v.box[3]);
+    t.box4 = v.box[4];
+    t.box5 = v.box[5];
+    t.depth = v.depth;
+    t.pad = 0;
+    return t;
+}
+
+__device__ __forceinline__ NodeVals from_tile(const TileVals& t) {
+    NodeVals v;
+    v.cm = t.cm;
+    v.col = t.col;
+    v.box[0] = t.box03.x;
+    v.box[1] = t.box03.y;
+    v.box[2] = t.box03.z;
+    v.box[3] = t.box03.w;
+    v.box[4] = t.box4;
+    v.box[5] = t.box5;
+    v.depth = t.depth;
+    return v;
+}
+
+// block-scope release/acquire add on a shared-memory counter
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(a), "r"(v) : "memory");
+    return old;
+}
+
+#define FILL_TILE 512
+
+// Tiled fill.  Block k owns the sorted slots [k T, k T + T) (T = FILL_TILE).
+// Phase 1: every thread initialises its leaf and keeps its values in shared
+// memory.  Phase 2: the leaf threads climb while the node's leaf range lies
+// inside the tile; the second child to arrive (a shared-memory counter)
+// combines the children from shared memory.  A thread whose next node crosses
+// a tile boundary hands its node to k_fill_top through a frontier list and
+// ends, so no block waits on a long climb.  The arithmetic of a node depends
+// only on its two children, so the result is the same in any schedule.
+__global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
+    extern __shared__ __align__(16) unsigned char fill_smem[];
+    TileVals* s_leaf = reinterpret_cast<TileVals*>(fill_smem);  // [FILL_TILE]
+    TileVals* s_node = s_leaf + FILL_TILE;                       // [FILL_TILE]
+    uint4* s_topo = reinterpret_cast<uint4*>(s_node + FILL_TILE);  // childA, childB, first slot, bodies
+    uint32_t* s_parent = reinterpret_cast<uint32_t*>(s_topo + FILL_TILE);
+    uint32_t* s_ready = s_parent + FILL_TILE;
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= n) return;
+    const uint32_t base = blockIdx.x * FILL_TILE;
+    const uint32_t t = threadIdx.x;
+    const uint32_t g = base + t;
+    if (base >= n) return;
     const gbh_sim_values* sim = b.sim;
-    const uint32_t bi = b.idx_in[g];
-    const float4 pm = ld_pos_mass(b.bodies_in, bi);
-    const float4 vd = ld_vel_density(b.bodies_in, bi);
-    // leaf init, bh_tree.comp:153-166
-    gbh_node* lf = &b.leaf[g];
-    float4* lp = reinterpret_cast<float4*>(lf);
-    const uint32_t parent0 = lf->parent_id;
-    NodeVals own;
-    own.cm = pm;
-    own.box[0] = own.box[3] = pm.x;
-    own.box[1] = own.box[4] = pm.y;
-    own.box[2] = own.box[5] = pm.z;
-    own.col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    own.depth = 0;
-    if (pm.w > 0.0f && vd.w > 0.0f) {
-        float rgb[3];
-        star_color(pm.w * sim->unit_mass, vd.w * sim->unit_density, rgb);
-        own.col = make_float4(rgb[0], rgb[1], rgb[2], 0.0f);
+    s_ready[t] = 0u;
+    if (g + 1 < n) {
+        // topology of internal node g (written by the build), read once
+        const gbh_node* nd = &b.internal[g];
+        const uint2 kids = __ldg(reinterpret_cast<const uint2*>(&nd->child_a));
+        s_topo[t] = make_uint4(kids.x, kids.y, __ldg(&b.node_lo[g]), __ldg(&nd->bodies_contained));
+        s_parent[t] = __ldg(&nd->parent_id);
     }
-    lp[0] = pm;
-    lp[1] = make_float4(pm.x, pm.y, pm.z, pm.x);
-    reinterpret_cast<uint4*>(lp)[2] = make_uint4(__float_as_uint(pm.y), __float_as_uint(pm.z), GBH_NONE, GBH_NONE);
-    reinterpret_cast<uint4*>(lp)[3] = make_uint4(0u, 0u, GBH_NONE, parent0);
-    lp[4] = own.col;
-    b.leaf_pm[g] = pm;
-    if (b.params->merging_collision_or_neither != GBH_MODE_NEITHER)
-        b.leaf_rad[g] = body_radius(sim->body_length_constant, pm.w, vd.w);
+    NodeVals own;
+    uint32_t parent0 = GBH_NONE;
+    if (g < n) {
+        const uint32_t bi = b.idx_in[g];
+        const float4 pm = ld_pos_mass(b.bodies_in, bi);
+        const float4 vd = ld_vel_density(b.bodies_in, bi);
+        // leaf init, bh_tree.comp:153-166
+        gbh_node* lf = &b.leaf[g];
+        float4* lp = reinterpret_cast<float4*>(lf);
+        parent0 = lf->parent_id;
+        own.cm = pm;
+        own.box[0] = own.box[3] = pm.x;
+        own.box[1] = own.box[4] = pm.y;
+        own.box[2] = own.box[5] = pm.z;
+        own.col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        own.depth = 0;
+        if (pm.w > 0.0f && vd.w > 0.0f) {
+            float rgb[3];
+            star_color(pm.w * sim->unit_mass, vd.w * sim->unit_density, rgb);
+            own.col = make_float4(rgb[0], rgb[1], rgb[2], 0.0f);
+        }
+        lp[0] = pm;
+        lp[1] = make_float4(pm.x, pm.y, pm.z, pm.x);
+        reinterpret_cast<uint4*>(lp)[2] = make_uint4(__float_as_uint(pm.y), __float_as_uint(pm.z), GBH_NONE, GBH_NONE);
+        reinterpret_cast<uint4*>(lp)[3] = make_uint4(0u, 0u, GBH_NONE, parent0);
+        lp[4] = own.col;
+        b.leaf_pm[g] = pm;
+        if (b.params->merging_collision_or_neither != GBH_MODE_NEITHER)
+            b.leaf_rad[g] = body_radius(sim->body_length_constant, pm.w, vd.w);
+        s_leaf[t] = to_tile(own);
+    }
+    __syncthreads();
+    if (g >= n) return;
+    const uint32_t tile_end = min(base + FILL_TILE, n);
 
-    // climb: the second child to arrive at a node finishes it
-    uint32_t self = g;          // global id of the node whose values are in `own`
+    uint32_t self = g;  // global id of the node whose values are in `own`
     uint32_t self_count = 1;
     uint32_t node = parent0;
+    // phase 2: nodes inside the tile (never for a single-body tree, whose root
+    // has one child)
+    while (n > 1 && node != GBH_NONE) {
+        const uint32_t i = node - N;
+        if (i < base || i >= tile_end) break;
+        const uint4 topo = s_topo[i - base];  // childA, childB, first slot, bodies
+        if (topo.z < base || topo.z + topo.w > tile_end) break;
+        if (atomic_add_acq_rel_cta(&s_ready[i - base], 1u) == 0u) return;
+        const bool self_is_a = topo.x == self;
+        const uint32_t sib = self_is_a ? topo.y : topo.x;
+        // the sibling lies inside the tile too
+        uint32_t sib_count = 1;
+        NodeVals S;
+        if (sib < N) {
+            S = from_tile(s_leaf[sib - base]);
+        } else {
+            S = from_tile(s_node[sib - N - base]);
+            sib_count = s_topo[sib - N - base].w;
+        }
+        const NodeVals& L = self_is_a ? own : S;
+        const NodeVals& R = self_is_a ? S : own;
+        const NodeVals out = combine(L, R);
+        const uint32_t a_id = self_is_a ? self : sib, b_id = self_is_a ? sib : self;
+        store_internal(b, i, out, L, R, a_id, b_id, self_is_a ? self_count : sib_count,
+                       self_is_a ? sib_count : self_count);
+        s_node[i - base] = to_tile(out);
+        self = node;
+        self_count += sib_count;
+        own = out;
+        node = s_parent[i - base];
+        if (node == GBH_NONE) {
+            b.st->tree_height = out.depth;
+            *b.root_rec = make_rec(out, self, self_count, false);
+            return;
+        }
+    }
+    // the next node crosses a tile boundary: hand over
+    if (node != GBH_NONE) {
+        const uint32_t slot = atomicAdd(&b.st->fill_frontier, 1u);
+        if (slot < b.fill_frontier_cap)
+            b.fill_frontier[slot] = make_uint2(self, self_count);
+        else
+            set_error(b.st, GBH_DEVERR_FILL_SPIN);
+    }
+}
+
+// Climb from node `self` (values `own`, `self_count` bodies) through the
+// global counters readyChildren (release/acquire at GPU scope): the second
+// arriving child reads its sibling from L2 and finishes the node.
+__device__ void climb_global(const StepBuffers& b, uint32_t self, uint32_t self_count, NodeVals own,
+                             uint32_t node) {
+    const uint32_t N = b.N;
     while (node != GBH_NONE) {
         const uint32_t i = node - N;
         gbh_node* nd = &b.internal[i];
@@ -218,46 +397,10 @@ __global__ __launch_bounds__(256) void k_fill(StepBuffers b) {
         }
         const NodeVals& L = self_is_a ? own : S;
         const NodeVals& R = self_is_a ? S : own;
-        // bh_tree.comp:223-246
-        const float lw = L.cm.w, rw = R.cm.w;
-        const float M = lw + rw;
-        NodeVals out;
-        if (M > 0.0f) {
-            out.cm.x = (lw * L.cm.x + rw * R.cm.x) / M;
-            out.cm.y = (lw * L.cm.y + rw * R.cm.y) / M;
-            out.cm.z = (lw * L.cm.z + rw * R.cm.z) / M;
-            out.col.x = (lw * L.col.x + rw * R.col.x) / M;
-            out.col.y = (lw * L.col.y + rw * R.col.y) / M;
-            out.col.z = (lw * L.col.z + rw * R.col.z) / M;
-        } else {
-            out.cm.x = (L.cm.x + R.cm.x) * 0.5f;
-            out.cm.y = (L.cm.y + R.cm.y) * 0.5f;
-            out.cm.z = (L.cm.z + R.cm.z) * 0.5f;
-            out.col.x = (L.col.x + R.col.x) * 0.5f;
-            out.col.y = (L.col.y + R.col.y) * 0.5f;
-            out.col.z = (L.col.z + R.col.z) * 0.5f;
-        }
-        out.cm.w = M;
-        out.col.w = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            out.box[k] = gmin(L.box[k], R.box[k]);
-            out.box[3 + k] = gmax(L.box[3 + k], R.box[3 + k]);
-        }
-        out.depth = 1u + max(L.depth, R.depth);
-        float4* np = reinterpret_cast<float4*>(nd);
-        __stcg(np + 0, out.cm);
-        __stcg(np + 1, make_float4(out.box[0], out.box[1], out.box[2], out.box[3]));
-        __stcg(reinterpret_cast<float2*>(np + 2), make_float2(out.box[4], out.box[5]));
-        nd->node_depth = out.depth;
-        nd->ready_children = GBH_NONE;
-        __stcg(np + 4, out.col);
-        // walk records of both children
-        ChildPair pr;
+        const NodeVals out = combine(L, R);
         const uint32_t a_id = self_is_a ? self : sib, b_id = self_is_a ? sib : self;
-        pr.a = make_rec(L, a_id, self_is_a ? self_count : sib_count, a_id < N);
-        pr.b = make_rec(R, b_id, self_is_a ? sib_count : self_count, b_id < N);
-        b.pairs[i] = pr;
+        store_internal(b, i, out, L, R, a_id, b_id, self_is_a ? self_count : sib_count,
+                       self_is_a ? sib_count : self_count);
         self = node;
         self_count = self_count + sib_count;
         own = out;
@@ -271,4 +414,25 @@ __global__ __launch_bounds__(256) void k_fill(StepBuffers b) {
     }
 }
 
-void launch_fill(const StepBuffers& b, cudaStream_t s) { k_fill<<<(b.N + 255) / 256, 256, 0, s>>>(b); }
+// Top-tree fill: the nodes that cross tile boundaries (about 2 N / FILL_TILE),
+// climbing from the frontier the tiled fill left.
+__global__ __launch_bounds__(256) void k_fill_top(StepBuffers b) {
+    const uint32_t count = min(b.st->fill_frontier, b.fill_frontier_cap);
+    const uint32_t N = b.N;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+        const uint2 fr = b.fill_frontier[e];
+        const gbh_node* nd = fr.x < N ? &b.leaf[fr.x] : &b.internal[fr.x - N];
+        climb_global(b, fr.x, fr.y, load_node_cg(nd), __ldcg(&nd->parent_id));
+    }
+}
+
+#define FILL_SMEM (FILL_TILE * (2 * sizeof(TileVals) + sizeof(uint4) + 2 * sizeof(uint32_t)))
+
+void fill_setup() {
+    cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FILL_SMEM);
+}
+
+void launch_fill(const StepBuffers& b, cudaStream_t s) {
+    k_fill<<<(b.N + FILL_TILE - 1) / FILL_TILE, FILL_TILE, FILL_SMEM, s>>>(b);
+    k_fill_top<<<152 * 4, 256, 0, s>>>(b);
+}
