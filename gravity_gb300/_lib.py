@@ -42,6 +42,10 @@ def _declare(L):
         "gbh_read_merge_tasks": [vp, vp, u32, C.POINTER(u32)],
         "gbh_read_accel": [vp, vp, u32, u32],
         "gbh_read_stats": [vp, C.POINTER(abi.Stats)],
+        "gbh_read_potential": [vp, vp, u32, u32],
+        "gbh_read_positions_fp64": [vp, vp, u32, u32],
+        "gbh_write_positions_fp64": [vp, vp, u32, u32],
+        "gbh_read_diagnostics": [vp, C.POINTER(abi.Diagnostics)],
         "gbh_device_ptrs": [vp, C.POINTER(abi.DeviceBuffers)],
         "gbh_write_sim_values": [vp, C.POINTER(abi.SimValues)],
         "gbh_write_index": [vp, vp, u32, u32],

@@ -33,6 +33,7 @@ BOUNDS_STATIC, BOUNDS_DYNAMIC = 0, 1
 MAC_PLAIN, MAC_LEARNED, MAC_GROUP = 0, 1, 2
 PRECISION_FP32, PRECISION_COMPENSATED = 0, 1
 FLAG_STORE_ACCEL = 0x1
+FLAG_STORE_POTENTIAL = 0x2
 BODIES_IN, BODIES_OUT = 0, 1
 NUM_STAGES = 8
 STAGE_NAMES = ("reset", "prepare", "sort", "build", "fill", "walk", "merge", "swap")
@@ -144,6 +145,27 @@ class Stats(C.Structure):
     ]
 
 
+class Diagnostics(C.Structure):
+    """gbh_diagnostics: conserved quantities summed in FP64."""
+
+    _fields_ = [
+        ("mass", C.c_double),
+        ("momentum", C.c_double * 3),
+        ("centre_of_mass", C.c_double * 3),
+        ("kinetic_energy", C.c_double),
+        ("potential_energy", C.c_double),
+        ("total_energy", C.c_double),
+        ("angular_momentum", C.c_double * 3),
+        ("live_bodies", C.c_uint32),
+        ("potential_valid", C.c_uint32),
+        ("positions_fp64", C.c_uint32),
+        ("pad", C.c_uint32),
+    ]
+
+
+assert C.sizeof(Diagnostics) == 13 * 8 + 16
+
+
 class DeviceBuffers(C.Structure):
     _fields_ = [
         ("bodies_in", C.c_void_p),
@@ -183,6 +205,16 @@ def step_params(
         dt, theta, softening, elasticity, restitution, mode, bounds, int(bool(wrap)), u, mac, precision,
         mac_tolerance, flags,
     )
+
+
+def diagnostics_to_dict(d: Diagnostics) -> dict:
+    out = {}
+    for name, _ in Diagnostics._fields_:
+        if name == "pad":
+            continue
+        v = getattr(d, name)
+        out[name] = list(v) if isinstance(v, C.Array) else v
+    return out
 
 
 def sim_to_dict(s: SimValues) -> dict:

@@ -210,6 +210,43 @@ class BarnesHut:
         self._chk(lib().gbh_direct_sum(self._h, C.byref(params), _ptr(s), len(s), _ptr(out)))
         return out
 
+    def read_potential(self, count=None, offset=0) -> np.ndarray:
+        count = self.n - offset if count is None else count
+        out = np.zeros(count, dtype=np.float32)
+        self._chk(lib().gbh_read_potential(self._h, _ptr(out), count, offset))
+        return out
+
+    def read_positions_fp64(self, count=None, offset=0) -> np.ndarray:
+        """FP64 positions of the precision form, float64[count, 3] by body id."""
+        count = self.n - offset if count is None else count
+        out = np.zeros((count, 4), dtype=np.float64)
+        self._chk(lib().gbh_read_positions_fp64(self._h, _ptr(out), count, offset))
+        return out[:, :3]
+
+    def write_positions_fp64(self, xyz: np.ndarray, offset: int = 0):
+        """Set FP64 positions (float64[count, 3]) of bodies [offset, offset + count);
+        their FP32 body positions become the rounded values."""
+        a = np.zeros((len(xyz), 4), dtype=np.float64)
+        a[:, :3] = xyz
+        self._chk(lib().gbh_write_positions_fp64(self._h, _ptr(a), len(a), offset))
+
+    def diagnostics(self, params: abi.StepParams | None = None) -> dict:
+        """Mass, momentum, centre of mass, kinetic/potential/total energy and
+        angular momentum of the current state in FP64.  With `params`, a walk
+        of the current state (state not advanced) supplies the potential."""
+        if params is not None:
+            p = abi.StepParams.from_buffer_copy(params)
+            p.flags |= abi.FLAG_STORE_POTENTIAL
+            self.reset_values(p)
+            self.partition_dead_bodies(p)
+            self.radix_sort()
+            self.build_binary_radix_tree()
+            self.compute_com_and_location()
+            self.compute_force(p)
+        d = abi.Diagnostics()
+        self._chk(lib().gbh_read_diagnostics(self._h, C.byref(d)))
+        return abi.diagnostics_to_dict(d)
+
     def evaluate_walk(self, params: abi.StepParams) -> np.ndarray:
         """Accelerations of the current state under `params` (tree + walk
         stages, no merge, no swap: the state does not advance).  float[N, 3]

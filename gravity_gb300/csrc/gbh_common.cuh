@@ -102,6 +102,12 @@ struct StepBuffers {
     uint2* groups;        // (first slot, body count) of the group walk's body groups
     uint2* fill_frontier; // (node, bodies) handed from the tiled fill to the top-tree fill
     uint32_t fill_frontier_cap;
+    // precision form (GBH_PRECISION_COMPENSATED); null until first used
+    const double* pos64_in;  // [N][4] FP64 positions (x, y, z, 0) by body id, current state
+    double* pos64_out;       // the next state's
+    float4* leaf_lo;         // by sorted slot: FP32 residual x64 - (float)x64 of the leaf's body
+    float* potential;        // walk potential by body id (GBH_FLAG_STORE_POTENTIAL)
+    uint32_t prec;           // 1: this step runs the precision form
     // compaction scratch
     uint32_t* tile_dead;
     float* tile_aabb;
@@ -149,6 +155,23 @@ __device__ __forceinline__ uint64_t morton_encode(float px, float py, float pz, 
         float nrm = (pos - mn[k]) / ext;
         float f = gclamp(floorf(nrm * 2097151.0f), 0.0f, 2097151.0f);
         q[k] = (uint32_t)floorf(f);
+    }
+    return (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
+}
+
+// The same quantisation from an FP64 position (the precision form): the
+// normalisation (x - min) / extent runs in FP64 about the FP32 box.
+__device__ __forceinline__ uint64_t morton_encode64(const double* p64, const float* mn, const float* mx) {
+    uint32_t q[3];
+    const bool empty = mn[0] > mx[0];
+    const bool centre = empty || !(isfinite(p64[0]) && isfinite(p64[1]) && isfinite(p64[2]));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double lo = mn[k], hi = mx[k];
+        const double pos = centre ? 0.5 * (lo + hi) : fmin(fmax(p64[k], lo), hi);
+        const double ext = fmax(hi - lo, 1e-9);
+        const double f = fmin(fmax(floor((pos - lo) / ext * 2097151.0), 0.0), 2097151.0);
+        q[k] = (uint32_t)f;
     }
     return (expand_bits21(q[0]) << 2) | (expand_bits21(q[1]) << 1) | expand_bits21(q[2]);
 }
@@ -212,6 +235,51 @@ __device__ __forceinline__ void walk_update(const StepBuffers& b, const gbh_step
     st_body(b.bodies_out, bi, make_float4(npx, npy, npz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
 }
 
+// The update of the precision form: the kick in FP32 as above, the drift in
+// FP64 from the FP64 position (pos64_in -> pos64_out); the body buffer gets
+// the FP32 rounding of the new position.  Static bounds as walk_update, the
+// wrap in FP64.
+__device__ __forceinline__ void walk_update_fp64(const StepBuffers& b, const gbh_step_params* P,
+                                                 const gbh_sim_values* sim, uint32_t bi, float4 pm, float4 vd,
+                                                 float ax, float ay, float az) {
+    const float dt = P->dt;
+    const float nvx = vd.x + ax * dt, nvy = vd.y + ay * dt, nvz = vd.z + az * dt;
+    const double2 xy = reinterpret_cast<const double2*>(b.pos64_in)[2 * (size_t)bi];
+    const double z0 = b.pos64_in[4 * (size_t)bi + 2];
+    double px = xy.x + (double)nvx * (double)dt;
+    double py = xy.y + (double)nvy * (double)dt;
+    double pz = z0 + (double)nvz * (double)dt;
+    if (P->static_or_dynamic == GBH_BOUNDS_STATIC) {
+        const float* mn = sim->bounds_min;
+        const float* mx = sim->bounds_max;
+        if (P->wrap_around) {
+            double x, y;
+            x = px - mn[0]; y = (double)mx[0] - mn[0]; px = (x - y * floor(x / y)) + mn[0];
+            x = py - mn[1]; y = (double)mx[1] - mn[1]; py = (x - y * floor(x / y)) + mn[1];
+            x = pz - mn[2]; y = (double)mx[2] - mn[2]; pz = (x - y * floor(x / y)) + mn[2];
+        } else if (pm.x < mn[0] || pm.x > mx[0] || pm.y < mn[1] || pm.y > mx[1] || pm.z < mn[2] || pm.z > mx[2]) {
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            st_body(b.bodies_out, bi, z, z);
+            reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi] = make_double2(0.0, 0.0);
+            reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi + 1] = make_double2(0.0, 0.0);
+            atomicAdd(&b.sim->out_of_bounds, 1u);
+            atomicAdd(&b.st->oob, 1u);
+            return;
+        }
+    }
+    reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi] = make_double2(px, py);
+    reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi + 1] = make_double2(pz, 0.0);
+    st_body(b.bodies_out, bi, make_float4((float)px, (float)py, (float)pz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
+}
+
+// Kahan-compensated accumulation (sum, c): sum + (x - c), c the lost low part
+__device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
+    const float y = x - c;
+    const float t = sum + y;
+    c = (t - sum) - y;
+    sum = t;
+}
+
 // ---- launchers (host), one translation unit each -----------------------------
 void launch_reset(const StepBuffers& b, cudaStream_t s);
 void launch_prepare(const StepBuffers& b, cudaStream_t s);
@@ -219,6 +287,13 @@ void launch_sort(const StepBuffers& b, cudaStream_t s);
 void launch_build(const StepBuffers& b, cudaStream_t s);
 void launch_fill(const StepBuffers& b, cudaStream_t s);
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s);
+void launch_init_pos64(const gbh_body* bodies, double* pos64, uint32_t N, cudaStream_t s);
+void launch_round_pos64(gbh_body* bodies, const double* pos64, uint32_t offset, uint32_t count, cudaStream_t s);
+void launch_direct_sum64(const double* pos64, const gbh_body* bodies, uint32_t nb, const uint32_t* sample,
+                         uint32_t count, double G, double soft, double* partial, double* out, uint32_t chunks,
+                         cudaStream_t s);
+void launch_diagnostics(const gbh_body* bodies, uint32_t nb, const double* pos64, const float* potential,
+                        double* partial, uint32_t blocks, double* out, cudaStream_t s);
 void launch_merge(const StepBuffers& b, cudaStream_t s);
 void launch_init_index(uint32_t* idx, uint32_t N, gbh_sim_values* sim, const gbh_units* units_dev, cudaStream_t s);
 void launch_direct_sum(const gbh_body* bodies, uint32_t n_bodies, const uint32_t* sample, uint32_t count,

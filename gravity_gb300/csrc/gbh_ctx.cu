@@ -79,6 +79,11 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     // sorted keys are back in keys_in, until the next step's encode)
     b.fill_frontier = reinterpret_cast<uint2*>(c->keys[1 - c->iin]);
     b.fill_frontier_cap = c->N;
+    b.pos64_in = c->pos64[c->bin];
+    b.pos64_out = c->pos64[1 - c->bin];
+    b.leaf_lo = c->leaf_lo;
+    b.potential = c->potential;
+    b.prec = (c->params_valid && c->params_host.precision_mode == GBH_PRECISION_COMPENSATED && c->pos64[0]) ? 1u : 0u;
     b.tile_dead = c->tile_dead;
     b.tile_aabb = c->tile_aabb;
     b.hist = c->hist;
@@ -159,6 +164,39 @@ static int enqueue_step(gbh_ctx* c) {
     return GBH_OK;
 }
 
+// FP64 positions (two, following the body buffers), leaf residuals and the
+// potential: 84 bytes per body, allocated when first needed.  Captured graphs
+// hold the old (null) pointers, so they are dropped.
+static int ensure_precision_buffers(gbh_ctx* c) {
+    if (c->pos64[0]) return GBH_OK;
+    const size_t n = c->N;
+    CUDA_TRY(c, cudaMalloc(&c->pos64[0], n * 32));
+    CUDA_TRY(c, cudaMalloc(&c->pos64[1], n * 32));
+    CUDA_TRY(c, cudaMalloc(&c->leaf_lo, n * 16));
+    CUDA_TRY(c, cudaMalloc(&c->potential, n * 4));
+    CUDA_TRY(c, cudaMemsetAsync(c->potential, 0, n * 4, c->stream));
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    c->pos64_valid = false;
+    return GBH_OK;
+}
+
+// Before a precision-form step: FP64 positions from the body buffer when they
+// are not current (first such step, after an upload or an FP32 step).
+static int prepare_precision(gbh_ctx* c) {
+    if (c->params_host.precision_mode != GBH_PRECISION_COMPENSATED || c->pos64_valid) return GBH_OK;
+    launch_init_pos64(c->bodies[c->bin], c->pos64[c->bin], c->N, c->stream);
+    c->pos64_valid = true;
+    return check_launch(c, "init fp64 positions");
+}
+
+// After the state advanced (swap): the FP64 positions are current only after
+// a precision-form walk.
+static void after_swap(gbh_ctx* c, bool precision_walk) {
+    c->pos64_valid = precision_walk && c->pos64[0] != nullptr;
+    ++c->state_epoch;
+}
+
 static int upload_params(gbh_ctx* c, const gbh_step_params* p) {
     if (!p) return fail(c, GBH_ERR_INVALID, "null step params");
     if (p->merging_collision_or_neither > 2 || p->static_or_dynamic > 1 || p->mac_mode > 2 || p->precision_mode > 1)
@@ -168,6 +206,12 @@ static int upload_params(gbh_ctx* c, const gbh_step_params* p) {
         return fail(c, GBH_ERR_STATE, "learned MAC selected but no weights were set");
     if (p->mac_mode != GBH_MAC_PLAIN && p->merging_collision_or_neither != GBH_MODE_NEITHER)
         return fail(c, GBH_ERR_UNSUPPORTED, "group and learned acceptance criteria run gravity only (no merges or collisions)");
+    if (p->precision_mode == GBH_PRECISION_COMPENSATED && p->merging_collision_or_neither != GBH_MODE_NEITHER)
+        return fail(c, GBH_ERR_UNSUPPORTED, "the precision form runs gravity only (no merges or collisions)");
+    if (p->precision_mode == GBH_PRECISION_COMPENSATED || (p->flags & GBH_FLAG_STORE_POTENTIAL)) {
+        int rc = ensure_precision_buffers(c);
+        if (rc) return rc;
+    }
     // pageable source: the copy is staged before cudaMemcpyAsync returns
     if (!c->params_valid || memcmp(&c->params_host, p, sizeof(*p)) != 0) {
         CUDA_TRY(c, cudaMemcpyAsync(c->params_dev, p, sizeof(*p), cudaMemcpyHostToDevice, c->stream));
@@ -298,6 +342,10 @@ int gbh_destroy(gbh_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     mac_release(c);
+    cudaFree(c->pos64[0]);
+    cudaFree(c->pos64[1]);
+    cudaFree(c->leaf_lo);
+    cudaFree(c->potential);
     if (c->arena) cudaFree(c->arena);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -311,6 +359,8 @@ int gbh_upload_bodies(gbh_ctx* c, const gbh_body* host, uint32_t count, uint32_t
     CUDA_TRY(c, cudaMemcpyAsync(c->bodies[c->bin] + offset, host, (size_t)count * sizeof(gbh_body),
                                 cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->pos64_valid = false;
+    ++c->state_epoch;
     return GBH_OK;
 }
 
@@ -325,7 +375,10 @@ int gbh_init(gbh_ctx* c) {
     return GBH_OK;
 }
 
-static int graph_key(const gbh_ctx* c) { return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2); }
+static int graph_key(const gbh_ctx* c) {
+    return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2) |
+           ((c->params_host.precision_mode == GBH_PRECISION_COMPENSATED) ? 16 : 0);
+}
 
 int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1); }
 
@@ -335,7 +388,9 @@ int gbh_step_n(gbh_ctx* c, const gbh_step_params* p, uint32_t count) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = upload_params(c, p);
     if (rc) return rc;
+    const bool prec = c->params_host.precision_mode == GBH_PRECISION_COMPENSATED;
     for (uint32_t s = 0; s < count; ++s) {
+        if ((rc = prepare_precision(c))) return rc;
         const int key = graph_key(c);
         auto it = c->graphs.find(key);
         if (it == c->graphs.end()) {
@@ -361,6 +416,7 @@ int gbh_step_n(gbh_ctx* c, const gbh_step_params* p, uint32_t count) {
         // the step flips both the body buffers and the (morton, index) buffers
         c->bin = 1 - c->bin;
         c->iin = 1 - c->iin;
+        after_swap(c, prec);
     }
     return GBH_OK;
 }
@@ -460,6 +516,68 @@ int gbh_read_accel(gbh_ctx* c, float* host, uint32_t count, uint32_t offset) {
     return read_dev(c, host, c->accel + offset, (size_t)count * 16);
 }
 
+int gbh_read_potential(gbh_ctx* c, float* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    if (!c->potential) return fail(c, GBH_ERR_STATE, "no potential (step with GBH_FLAG_STORE_POTENTIAL first)");
+    return read_dev(c, host, c->potential + offset, (size_t)count * 4);
+}
+
+int gbh_read_positions_fp64(gbh_ctx* c, double* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    if (!c->pos64[0] || !c->pos64_valid) return fail(c, GBH_ERR_STATE, "FP64 positions are not current");
+    return read_dev(c, host, c->pos64[c->bin] + 4 * (size_t)offset, (size_t)count * 32);
+}
+
+int gbh_write_positions_fp64(gbh_ctx* c, const double* host, uint32_t count, uint32_t offset) {
+    RANGE_CHECK(c, host, count, offset, c->N);
+    int rc = ensure_precision_buffers(c);
+    if (rc) return rc;
+    if (!c->pos64_valid) {
+        launch_init_pos64(c->bodies[c->bin], c->pos64[c->bin], c->N, c->stream);
+        if ((rc = check_launch(c, "init fp64 positions"))) return rc;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c->pos64[c->bin] + 4 * (size_t)offset, host, (size_t)count * 32,
+                                cudaMemcpyHostToDevice, c->stream));
+    launch_round_pos64(c->bodies[c->bin], c->pos64[c->bin], offset, count, c->stream);
+    if ((rc = check_launch(c, "round fp64 positions"))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->pos64_valid = true;
+    ++c->state_epoch;
+    return GBH_OK;
+}
+
+int gbh_read_diagnostics(gbh_ctx* c, gbh_diagnostics* out) {
+    if (!c || !out) return GBH_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const bool pot = c->potential && c->potential_epoch == c->state_epoch;
+    const bool p64 = c->pos64[0] && c->pos64_valid;
+    const uint32_t blocks = 152 * 4;
+    double* d = nullptr;
+    CUDA_TRY(c, cudaMalloc(&d, (size_t)(blocks + 1) * 16 * 8));
+    launch_diagnostics(c->bodies[c->bin], c->N, p64 ? c->pos64[c->bin] : nullptr, pot ? c->potential : nullptr,
+                       d + 16, blocks, d, c->stream);
+    double v[16] = {0};
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v, d, 15 * 8, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(c, GBH_ERR_CUDA, std::string("diagnostics: ") + cudaGetErrorString(e));
+    memset(out, 0, sizeof(*out));
+    out->mass = v[0];
+    for (int k = 0; k < 3; ++k) {
+        out->momentum[k] = v[1 + k];
+        out->centre_of_mass[k] = v[0] != 0.0 ? v[4 + k] / v[0] : 0.0;
+        out->angular_momentum[k] = v[9 + k];
+    }
+    out->kinetic_energy = v[7];
+    out->potential_energy = pot ? v[8] : 0.0;
+    out->total_energy = out->kinetic_energy + out->potential_energy;
+    out->live_bodies = (uint32_t)v[12];
+    out->potential_valid = pot ? 1u : 0u;
+    out->positions_fp64 = p64 ? 1u : 0u;
+    return GBH_OK;
+}
+
 int gbh_read_stats(gbh_ctx* c, gbh_stats* s) {
     if (!c || !s) return GBH_ERR_INVALID;
     DevState st;
@@ -532,22 +650,39 @@ static int stage_common(gbh_ctx* c, const gbh_step_params* p) {
         return gbh_synchronize(c);    \
     } while (0)
 
-int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_reset); }
+int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) {
+    int rc = stage_common(c, p);
+    if (rc) return rc;
+    if ((rc = prepare_precision(c))) return rc;
+    if ((rc = enqueue_reset(c))) return rc;
+    return gbh_synchronize(c);
+}
 int gbh_stage_prepare(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_prepare); }
 int gbh_stage_sort(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_sort); }
 int gbh_stage_build(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_build); }
 int gbh_stage_fill(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_fill); }
-int gbh_stage_walk(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_walk); }
+int gbh_stage_walk(gbh_ctx* c, const gbh_step_params* p) {
+    int rc = stage_common(c, p);
+    if (rc) return rc;
+    if (c->params_host.precision_mode == GBH_PRECISION_COMPENSATED && !c->pos64_valid)
+        return fail(c, GBH_ERR_STATE, "precision-form walk without current FP64 positions (run gbh_stage_reset first)");
+    if ((rc = enqueue_walk(c))) return rc;
+    if (c->params_host.flags & GBH_FLAG_STORE_POTENTIAL) c->potential_epoch = c->state_epoch;
+    return gbh_synchronize(c);
+}
 int gbh_stage_merge(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_merge); }
 int gbh_stage_swap(gbh_ctx* c) {
     if (!c) return GBH_ERR_INVALID;
-    return enqueue_swap(c);
+    int rc = enqueue_swap(c);
+    after_swap(c, c->params_valid && c->params_host.precision_mode == GBH_PRECISION_COMPENSATED);
+    return rc;
 }
 
 int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM_STAGES]) {
     int rc = stage_common(c, p);
     if (rc) return rc;
     if (!ms_out) return fail(c, GBH_ERR_INVALID, "ms_out is null");
+    if ((rc = prepare_precision(c))) return rc;
     cudaEvent_t ev[GBH_NUM_STAGES + 1];
     for (int i = 0; i <= GBH_NUM_STAGES; ++i) CUDA_TRY(c, cudaEventCreate(&ev[i]));
     CUDA_TRY(c, cudaEventRecord(ev[0], c->stream));
@@ -562,6 +697,7 @@ int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM
     }
     for (int i = 0; i <= GBH_NUM_STAGES; ++i) cudaEventDestroy(ev[i]);
     if (rc) return rc;
+    after_swap(c, c->params_host.precision_mode == GBH_PRECISION_COMPENSATED);
     return gbh_synchronize(c);
 }
 
@@ -584,9 +720,14 @@ int gbh_direct_sum(gbh_ctx* c, const gbh_step_params* p, const uint32_t* sample,
     CUDA_TRY(c, cudaMalloc(&d_partial, (size_t)chunks * count * 3 * 8));
     CUDA_TRY(c, cudaMalloc(&d_out, (size_t)count * 3 * 8));
     cudaError_t e = cudaMemcpyAsync(d_sample, sample, (size_t)count * 4, cudaMemcpyHostToDevice, c->stream);
+    const bool fp64 = p->precision_mode == GBH_PRECISION_COMPENSATED && c->pos64_valid;
     if (e == cudaSuccess) {
-        launch_direct_sum(c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant, p->softening,
-                          d_partial, d_out, chunks, c->stream);
+        if (fp64)
+            launch_direct_sum64(c->pos64[c->bin], c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant,
+                                p->softening, d_partial, d_out, chunks, c->stream);
+        else
+            launch_direct_sum(c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant, p->softening,
+                              d_partial, d_out, chunks, c->stream);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, (size_t)count * 3 * 8, cudaMemcpyDeviceToHost, c->stream);

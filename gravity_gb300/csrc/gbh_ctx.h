@@ -49,6 +49,14 @@ struct gbh_ctx {
     uint32_t* lookback = nullptr;
     size_t lookback_bytes = 0;
 
+    // precision form and potential (allocated on first use, outside the arena)
+    double* pos64[2] = {nullptr, nullptr};  // follow the body buffers' parity
+    float4* leaf_lo = nullptr;
+    float* potential = nullptr;
+    bool pos64_valid = false;      // pos64[bin] holds the current state
+    uint64_t state_epoch = 0;      // advances with every swap and upload
+    uint64_t potential_epoch = ~0ull;  // state whose potential is in `potential`
+
     gbh_step_params params_host{};
     bool params_valid = false;
     uint32_t mac_mode = GBH_MAC_PLAIN;

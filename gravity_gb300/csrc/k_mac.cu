@@ -494,6 +494,7 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
     // 1. tree of the current state and the plain theta = 0.2 walk (accelerations)
     gbh_step_params p = *params;
     p.mac_mode = GBH_MAC_PLAIN;
+    p.precision_mode = GBH_PRECISION_FP32;
     p.theta = 0.2f;
     p.flags |= GBH_FLAG_STORE_ACCEL;
     rc = upload_step_params(c, p);

@@ -322,7 +322,8 @@ __global__ __launch_bounds__(PREP_THREADS) void k_prep_scatter(StepBuffers b) {
         if (alive[it]) {
             const uint32_t dst = alive_before_tile + arank;
             b.idx_out[dst] = bidx[it];
-            const uint64_t key = morton_encode(pm[it].x, pm[it].y, pm[it].z, s_mn, s_mx);
+            const uint64_t key = b.prec ? morton_encode64(b.pos64_in + 4 * (size_t)bidx[it], s_mn, s_mx)
+                                        : morton_encode(pm[it].x, pm[it].y, pm[it].z, s_mn, s_mx);
             b.keys_out[dst] = key;
 #pragma unroll
             for (int p = 0; p < SORT_PASSES; ++p) atomicAdd(&s_hist[p * SORT_RADIX + ((key >> (8 * p)) & 0xFF)], 1u);

@@ -310,6 +310,13 @@ __global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
         b.leaf_pm[g] = pm;
         if (b.params->merging_collision_or_neither != GBH_MODE_NEITHER)
             b.leaf_rad[g] = body_radius(sim->body_length_constant, pm.w, vd.w);
+        if (b.prec) {
+            // precision form: the FP32 residual of the FP64 position
+            const double2 xy = reinterpret_cast<const double2*>(b.pos64_in)[2 * (size_t)bi];
+            const double z = b.pos64_in[4 * (size_t)bi + 2];
+            b.leaf_lo[g] = make_float4((float)(xy.x - (double)pm.x), (float)(xy.y - (double)pm.y),
+                                       (float)(z - (double)pm.z), 0.0f);
+        }
         s_leaf[t] = to_tile(own);
     }
     __syncthreads();

@@ -37,6 +37,11 @@ struct __align__(16) StackEntry {
     uint32_t pad;
 };
 
+// PREC: the precision form.  Offsets are formed from the FP32 position and
+// its FP32 residual (leaf_lo), r = (x_j - x_b) + (lo_j - lo_b) for a leaf and
+// (com - x_b) - lo_b for a node, and the leaf terms are summed with Kahan
+// compensation apart from the node terms.  Gravity only.
+template <bool PREC>
 __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     __shared__ StackEntry s_stack[WALK_WARPS][WALK_STACK];
     const uint32_t n = b.st->n_new;
@@ -58,7 +63,11 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     float4 pm = active ? b.leaf_pm[g] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 vd = active ? ld_vel_density(b.bodies_in, bi) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float my_rad = (active && mode != GBH_MODE_NEITHER) ? b.leaf_rad[g] : 0.0f;
-    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    const float4 lo_b = (PREC && active) ? b.leaf_lo[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
+    float ax = 0.0f, ay = 0.0f, az = 0.0f, pot = 0.0f;
+    float nx_ = 0.0f, ny_ = 0.0f, nz_ = 0.0f, np_ = 0.0f;  // PREC: leaf terms (Kahan)
+    float cx_ = 0.0f, cy_ = 0.0f, cz_ = 0.0f, cp_ = 0.0f;
     uint32_t inter = 0, seq = 0;
     uint32_t opened = 0;
     uint32_t sp = 0, max_sp = 0;
@@ -78,7 +87,14 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     const bool walk = n > 1;
     while (walk) {
         const bool me = (cur_mask >> lane) & 1u;
-        const float rx = cur_cm.x - pm.x, ry = cur_cm.y - pm.y, rz = cur_cm.z - pm.z;
+        float rx = cur_cm.x - pm.x, ry = cur_cm.y - pm.y, rz = cur_cm.z - pm.z;
+        if (PREC) {
+            float4 lo_j = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (cur_id < N) lo_j = b.leaf_lo[cur_id];
+            rx = rx + (lo_j.x - lo_b.x);
+            ry = ry + (lo_j.y - lo_b.y);
+            rz = rz + (lo_j.z - lo_b.z);
+        }
         const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
         const float inv = rsqrtf(rr + soft);
         bool open = false, interact;
@@ -91,11 +107,19 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
         }
         if (interact) {
             const float f = G * cur_cm.w * (inv * inv * inv);
-            ax = __fmaf_rn(f, rx, ax);
-            ay = __fmaf_rn(f, ry, ay);
-            az = __fmaf_rn(f, rz, az);
+            if (PREC && cur_id < N) {
+                kahan_add(nx_, cx_, f * rx);
+                kahan_add(ny_, cy_, f * ry);
+                kahan_add(nz_, cz_, f * rz);
+                if (want_pot) kahan_add(np_, cp_, -(G * cur_cm.w) * inv);
+            } else {
+                ax = __fmaf_rn(f, rx, ax);
+                ay = __fmaf_rn(f, ry, ay);
+                az = __fmaf_rn(f, rz, az);
+                if (want_pot) pot = __fmaf_rn(-(G * cur_cm.w), inv, pot);
+            }
             ++inter;
-            if (mode != GBH_MODE_NEITHER && cur_id < N) {
+            if (!PREC && mode != GBH_MODE_NEITHER && cur_id < N) {
                 const uint32_t oi = b.idx_in[cur_id];
                 const float orad = b.leaf_rad[cur_id];
                 const float dist = sqrtf(rx * rx + ry * ry + rz * rz);
@@ -178,12 +202,25 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
         atomicMax(&b.st->max_stack, max_sp + 1);
     }
     if (!active) return;
+    if (PREC) {
+        ax = ax + (nx_ - cx_);
+        ay = ay + (ny_ - cy_);
+        az = az + (nz_ - cz_);
+        pot = pot + (np_ - cp_);
+    }
     if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
     if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
-    walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
+    if (want_pot) b.potential[bi] = pot;
+    if (PREC)
+        walk_update_fp64(b, P, sim, bi, pm, vd, ax, ay, az);
+    else
+        walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
 }
 
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s) {
     const uint32_t blocks = (b.N + WALK_THREADS - 1) / WALK_THREADS;
-    k_walk_plain<<<blocks, WALK_THREADS, 0, s>>>(b);
+    if (b.prec)
+        k_walk_plain<true><<<blocks, WALK_THREADS, 0, s>>>(b);
+    else
+        k_walk_plain<false><<<blocks, WALK_THREADS, 0, s>>>(b);
 }

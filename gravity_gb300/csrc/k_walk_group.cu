@@ -96,8 +96,13 @@ __global__ void k_find_groups(StepBuffers b) {
     }
 }
 
-template <int MODE>
-__global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_group(StepBuffers b, MacDeviceWeights mw) {
+// PREC: the precision form.  The lanes' bodies and the list entries are kept
+// relative to the group centre c_g: (x - c_g) + lo for a leaf (lo its FP32
+// residual), com - c_g for a node; leaf terms are summed with Kahan
+// compensation apart from the node terms.
+template <int MODE, bool PREC>
+__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) void k_walk_group(StepBuffers b,
+                                                                                             MacDeviceWeights mw) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Cfg = GroupCfg<MODE>;
     typename Cfg::Smem& S = *reinterpret_cast<typename Cfg::Smem*>(smem_raw);
@@ -151,7 +156,16 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         __syncwarp();
     }
 
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    // walk coordinates of this lane's body (absolute, or group-relative)
+    float4 pw = pm;
+    if (PREC) {
+        const float4 lo_b = b.leaf_lo[active ? g : grp.x];
+        pw = make_float4((pm.x - gg.cx) + lo_b.x, (pm.y - gg.cy) + lo_b.y, (pm.z - gg.cz) + lo_b.z, pm.w);
+    }
+    const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
+    float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
+    float nx_ = 0.f, ny_ = 0.f, nz_ = 0.f, np_ = 0.f;  // PREC: leaf terms (Kahan)
+    float cx_ = 0.f, cy_ = 0.f, cz_ = 0.f, cp_ = 0.f;
     uint32_t inter = 0, evals = 0, opened = 0;
     uint32_t sp = n > 1 ? 1u : 0u, ln = 0, np = 0;
     bool saturated = false;
@@ -163,11 +177,35 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
     // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
     const bool self_check = !(soft >= 1e-20f);
     auto flush = [&](uint32_t cnt) {
-        if (self_check) {
+        if (PREC || want_pot) {
+            // the general loop: leaf terms apart (PREC), potential, self check
+#pragma unroll 2
+            for (uint32_t j = 0; j < cnt; ++j) {
+                const float4 c = lcm[j];
+                const uint32_t lj = lid[j];
+                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
+                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                const float inv = rsqrtf(rr);
+                const bool self = self_check && lj == g;
+                const float f = self ? 0.0f : c.w * (inv * inv * inv);
+                const float ph = self ? 0.0f : -c.w * inv;
+                if (PREC && lj < N) {
+                    kahan_add(nx_, cx_, f * rx);
+                    kahan_add(ny_, cy_, f * ry);
+                    kahan_add(nz_, cz_, f * rz);
+                    if (want_pot) kahan_add(np_, cp_, ph);
+                } else {
+                    ax = __fmaf_rn(f, rx, ax);
+                    ay = __fmaf_rn(f, ry, ay);
+                    az = __fmaf_rn(f, rz, az);
+                    if (want_pot) pot += ph;
+                }
+            }
+        } else if (self_check) {
 #pragma unroll 4
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
-                const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
+                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
                 const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                 const float inv = rsqrtf(rr);
                 const float f = (lid[j] == g) ? 0.0f : c.w * (inv * inv * inv);
@@ -179,7 +217,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
 #pragma unroll 4
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
-                const float rx = c.x - pm.x, ry = c.y - pm.y, rz = c.z - pm.z;
+                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
                 const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                 const float inv = rsqrtf(rr);
                 const float f = c.w * (inv * inv * inv);
@@ -191,7 +229,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         inter += cnt;
     };
     // each lane's outcome: 1 list, 2 open (push children); warp-collective
-    auto commit = [&](uint32_t kind, uint32_t id, float4 cm, uint32_t ca, uint32_t cb) {
+    auto commit = [&](uint32_t kind, uint32_t id, float4 cm, uint32_t ca, uint32_t cb, float4 lo) {
         uint32_t bo = __ballot_sync(0xffffffffu, kind == 2);
         if (sp + 2 * __popc(bo) > (uint32_t)Cfg::stack) {
             // frontier full: accept instead of opening (less accurate, never wrong)
@@ -202,7 +240,10 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         const uint32_t bl = __ballot_sync(0xffffffffu, kind == 1);
         if (kind == 1) {
             const uint32_t pos = ln + __popc(bl & lanemask_lt());
-            lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
+            if (PREC)
+                lcm[pos] = make_float4((cm.x - gg.cx) + lo.x, (cm.y - gg.cy) + lo.y, (cm.z - gg.cz) + lo.z, G * cm.w);
+            else
+                lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
             lid[pos] = id;
         }
         ln += __popc(bl);
@@ -267,7 +308,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         }
         np = rest;
         __syncwarp();
-        commit(kind, id, cm, ca, cb);
+        commit(kind, id, cm, ca, cb, make_float4(0.f, 0.f, 0.f, 0.f));
     };
 
     while (sp > 0 || np > 0) {
@@ -282,11 +323,12 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         __syncwarp();
         uint32_t kind = 0;  // 0 nothing, 1 list, 2 open, 3 queued for the network
         float4 cm = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 qb0 = cm, qb1 = cm;
+        float4 qb0 = cm, qb1 = cm, lo = cm;
         uint32_t ca = 0, cb = 0, qcount = 0;
         if (has) {
             if (id < N) {
                 cm = b.leaf_pm[id];
+                if (PREC) lo = b.leaf_lo[id];
                 kind = 1;
             } else {
                 const gbh_node* nd = &b.internal[id - N];
@@ -344,7 +386,7 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         } else {
             evals += __popc(__ballot_sync(0xffffffffu, has && id >= N));
         }
-        commit(kind, id, cm, ca, cb);
+        commit(kind, id, cm, ca, cb, lo);
         if (MODE == GM_LEARNED && np >= 32) decide_queue(32);
     }
     if (ln) flush(ln);
@@ -358,10 +400,20 @@ __global__ __launch_bounds__(GW_THREADS, MODE == GM_THETA ? 4 : 3) void k_walk_g
         atomicAdd(&b.st->opened, (unsigned long long)opened);
     }
     if (active) {
+        if (PREC) {
+            ax = ax + (nx_ - cx_);
+            ay = ay + (ny_ - cy_);
+            az = az + (nz_ - cz_);
+            pot = pot + (np_ - cp_);
+        }
         if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
         if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
+        if (want_pot) b.potential[bi] = pot;
         const float4 vd = ld_vel_density(b.bodies_in, bi);
-        walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
+        if (PREC)
+            walk_update_fp64(b, P, sim, bi, pm, vd, ax, ay, az);
+        else
+            walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
     }
     __syncwarp();
     }  // groups
@@ -372,11 +424,17 @@ static size_t group_smem(int mode) {
                                                                               : GroupCfg<GM_THETA>::smem;
 }
 
+template <int MODE, bool PREC>
+static void set_smem() {
+    cudaFuncSetAttribute(k_walk_group<MODE, PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(MODE));
+}
+
 void group_walk_setup() {
-    cudaFuncSetAttribute(k_walk_group<GM_THETA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(GM_THETA));
-    cudaFuncSetAttribute(k_walk_group<GM_LEARNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)group_smem(GM_LEARNED));
-    cudaFuncSetAttribute(k_walk_group<GM_RECORD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(GM_RECORD));
+    set_smem<GM_THETA, false>();
+    set_smem<GM_THETA, true>();
+    set_smem<GM_LEARNED, false>();
+    set_smem<GM_LEARNED, true>();
+    set_smem<GM_RECORD, false>();
 }
 
 void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
@@ -384,21 +442,28 @@ void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
     k_find_groups<<<(b.N + 255) / 256, 256, 0, s>>>(b);
 }
 
-template <int MODE>
+template <int MODE, bool PREC>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
     if (MODE != GM_RECORD) launch_find_groups(b, s);
     const uint32_t blocks = (b.N + GW_THREADS - 1) / GW_THREADS;
-    k_walk_group<MODE><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
+    k_walk_group<MODE, PREC><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
 }
 
 void launch_walk_group(const StepBuffers& b, const MacDeviceWeights& mw, bool learned, cudaStream_t s) {
-    if (learned)
-        launch_mode<GM_LEARNED>(b, mw, s);
-    else
-        launch_mode<GM_THETA>(b, mw, s);
+    if (learned) {
+        if (b.prec)
+            launch_mode<GM_LEARNED, true>(b, mw, s);
+        else
+            launch_mode<GM_LEARNED, false>(b, mw, s);
+    } else {
+        if (b.prec)
+            launch_mode<GM_THETA, true>(b, mw, s);
+        else
+            launch_mode<GM_THETA, false>(b, mw, s);
+    }
 }
 
 // the caller runs launch_find_groups once first: pairs name groups by index
 void launch_walk_group_record(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
-    launch_mode<GM_RECORD>(b, mw, s);
+    launch_mode<GM_RECORD, false>(b, mw, s);
 }

@@ -50,7 +50,7 @@ extern "C" {
 
 /* ---- device error word bits (gbh_stats.error_word) ------------------------ */
 #define GBH_DEVERR_SORT_LOOKBACK 0x1u   /* onesweep look-back spin gave up (bounded wait) */
-#define GBH_DEVERR_FILL_SPIN 0x2u       /* reserved: bottom-up fill never spins, kept for ABI stability */
+#define GBH_DEVERR_FILL_SPIN 0x2u       /* bottom-up fill: frontier list overflow (cannot happen at its capacity N) */
 #define GBH_DEVERR_WALK_STACK 0x4u      /* a tree walk needed more stack than GBH_WALK_STACK */
 #define GBH_DEVERR_MERGE_OVERFLOW 0x8u  /* more conflicting merge tasks than one block can order */
 #define GBH_DEVERR_TREE_HEIGHT 0x10u    /* tree height above 64 (the reference fills only 64 levels) */
@@ -70,10 +70,20 @@ extern "C" {
 #define GBH_MAC_GROUP 2u    /* group theta rule used as the learned criterion's ablation */
 /* precision form (new in this library) */
 #define GBH_PRECISION_FP32 0u     /* reference arithmetic */
-#define GBH_PRECISION_COMPENSATED 1u /* FP64 drift + compensated FP32 force sums */
+/* GBH_PRECISION_COMPENSATED: FP64 positions on the device (the drift
+ * x += v dt runs in FP64; the body buffer holds their FP32 rounding), the
+ * Morton quantisation from the FP64 positions, and walk coordinates relative
+ * to the body (plain walk) or to the group centre (group walks) formed from
+ * the FP32 position plus its FP32 residual, with Kahan-compensated sums of
+ * the near field (leaf) terms.  Gravity only (merging_collision_or_neither 0).
+ * The FP64 positions start from the body buffer at the first such step and
+ * after every gbh_upload_bodies or FP32 step. */
+#define GBH_PRECISION_COMPENSATED 1u
 
 /* step flags */
-#define GBH_FLAG_STORE_ACCEL 0x1u  /* keep each body's walk acceleration (gbh_read_accel) */
+#define GBH_FLAG_STORE_ACCEL 0x1u      /* keep each body's walk acceleration (gbh_read_accel) */
+#define GBH_FLAG_STORE_POTENTIAL 0x2u  /* keep each body's walk potential (gbh_read_potential,
+                                          the potential energy of gbh_diagnostics) */
 
 /* ---- buffers, byte-identical to the reference std430 layouts -------------- */
 
@@ -230,6 +240,35 @@ int gbh_read_merge_tasks(gbh_ctx* ctx, uint32_t* host_pairs, uint32_t capacity, 
 /* walk acceleration per body index (needs GBH_FLAG_STORE_ACCEL): float[4] per body */
 int gbh_read_accel(gbh_ctx* ctx, float* host_xyzw, uint32_t count, uint32_t offset);
 int gbh_read_stats(gbh_ctx* ctx, gbh_stats* host);
+/* walk potential per body index (needs GBH_FLAG_STORE_POTENTIAL): float per body,
+ * sum over accepted nodes and leaves of -G m / sqrt(r.r + softening) */
+int gbh_read_potential(gbh_ctx* ctx, float* host, uint32_t count, uint32_t offset);
+/* FP64 positions of the precision form per body index: double[4] (x, y, z, 0) per
+ * body; GBH_ERR_STATE when they are not current */
+int gbh_read_positions_fp64(gbh_ctx* ctx, double* host_xyz0, uint32_t count, uint32_t offset);
+/* Set FP64 positions of the precision form (double[4] per body, the fourth
+ * ignored) for bodies [offset, offset + count); their FP32 body positions
+ * become the rounded values.  The other bodies keep their positions. */
+int gbh_write_positions_fp64(gbh_ctx* ctx, const double* host_xyz0, uint32_t count, uint32_t offset);
+
+/* Conserved quantities of the current state, summed in FP64 over the live
+ * bodies (positions from the FP64 copy when it is current).  The potential
+ * energy needs the potential of the last walk (GBH_FLAG_STORE_POTENTIAL);
+ * potential_valid says whether it was taken from the current state. */
+typedef struct gbh_diagnostics {
+    double mass;
+    double momentum[3];
+    double centre_of_mass[3];
+    double kinetic_energy;   /* sum 1/2 m v.v */
+    double potential_energy; /* 1/2 sum m phi */
+    double total_energy;
+    double angular_momentum[3]; /* about the origin: sum m x cross v */
+    uint32_t live_bodies;
+    uint32_t potential_valid;
+    uint32_t positions_fp64; /* 1 when the FP64 positions were used */
+    uint32_t pad;
+} gbh_diagnostics;
+int gbh_read_diagnostics(gbh_ctx* ctx, gbh_diagnostics* out);
 int gbh_device_ptrs(gbh_ctx* ctx, gbh_device_buffers* out);
 /* opaque cudaStream_t of the context */
 void* gbh_stream(gbh_ctx* ctx);
@@ -273,6 +312,8 @@ int gbh_step_profiled(gbh_ctx* ctx, const gbh_step_params* params, float ms_out[
  * Direct-sum accelerations for `count` sampled body indices against every live
  * body of the current state (terms in FP32, sums compensated in double-float).
  * out: double[3*count].  Uses G, softening from `params`. */
+/* With params->precision_mode == GBH_PRECISION_COMPENSATED and current FP64
+ * positions, the terms and sums are FP64 throughout (an FP64 direct sum). */
 int gbh_direct_sum(gbh_ctx* ctx, const gbh_step_params* params, const uint32_t* sample,
                    uint32_t count, double* out_accel);
 

@@ -54,9 +54,11 @@ PROBE = r"""
 #define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f))
 int main(void) {
   printf("sizeof.gbh_body %zu\nsizeof.gbh_node %zu\nsizeof.gbh_sim_values %zu\nsizeof.gbh_step_params %zu\n"
-         "sizeof.gbh_units %zu\nsizeof.gbh_stats %zu\nsizeof.gbh_device_buffers %zu\n",
+         "sizeof.gbh_units %zu\nsizeof.gbh_stats %zu\nsizeof.gbh_device_buffers %zu\n"
+         "sizeof.gbh_diagnostics %zu\noffsetof.diag.live_bodies %zu\n",
          sizeof(gbh_body), sizeof(gbh_node), sizeof(gbh_sim_values), sizeof(gbh_step_params),
-         sizeof(gbh_units), sizeof(gbh_stats), sizeof(gbh_device_buffers));
+         sizeof(gbh_units), sizeof(gbh_stats), sizeof(gbh_device_buffers),
+         sizeof(gbh_diagnostics), offsetof(gbh_diagnostics, live_bodies));
   P(gbh_node, child_a); P(gbh_node, parent_id); P(gbh_node, avg_color);
   P(gbh_sim_values, bounds_min); P(gbh_sim_values, bounds_max); P(gbh_sim_values, unit_mass);
   P(gbh_sim_values, gravitational_constant); P(gbh_sim_values, uint_debug); P(gbh_sim_values, float_debug);
@@ -82,6 +84,8 @@ def test_struct_layouts_match_header():
     assert got["sizeof.gbh_step_params"] == C.sizeof(abi.StepParams)
     assert got["sizeof.gbh_units"] == C.sizeof(abi.Units)
     assert got["sizeof.gbh_stats"] == C.sizeof(abi.Stats)
+    assert got["sizeof.gbh_diagnostics"] == C.sizeof(abi.Diagnostics)
+    assert got["offsetof.diag.live_bodies"] == abi.Diagnostics.live_bodies.offset
     assert got["sizeof.gbh_device_buffers"] == C.sizeof(abi.DeviceBuffers)
     assert got["gbh_node.child_a"] == 40 and got["gbh_node.parent_id"] == 60 and got["gbh_node.avg_color"] == 64
     assert got["gbh_sim_values.bounds_min"] == 32 and got["gbh_sim_values.bounds_max"] == 48
