@@ -21,7 +21,7 @@
 #define SORT_RADIX 256
 #define SORT_PASSES 8
 #define SORT_THREADS 256
-#define SORT_ITEMS 12
+#define SORT_ITEMS 16
 #define SORT_TILE (SORT_THREADS * SORT_ITEMS)
 
 // fused compaction / bounds / encode geometry

@@ -50,7 +50,7 @@ struct SortSmem {
     uint32_t vals[SORT_TILE];
 };
 
-__global__ __launch_bounds__(SORT_THREADS, 2) void k_sort_pass(StepBuffers b, uint32_t pass, const uint64_t* __restrict__ kin,
+__global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, uint32_t pass, const uint64_t* __restrict__ kin,
                                                                const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                                                uint32_t* __restrict__ vout) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -91,12 +91,11 @@ __global__ __launch_bounds__(SORT_THREADS, 2) void k_sort_pass(StepBuffers b, ui
         const uint32_t peers = __match_any_sync(0xffffffffu, dig);
         const uint32_t leader = __ffs(peers) - 1;
         const uint32_t before = __popc(peers & lanemask_lt());
-        const uint32_t cnt = __popc(peers);
-        const uint32_t prev = S.warp_hist[w][dig];
-        __syncwarp();
-        if (lane == leader) S.warp_hist[w][dig] = prev + cnt;
-        __syncwarp();
-        rank[i] = prev + before;
+        // the digit's leader reserves the group's ranks; a warp's shared
+        // memory atomics take effect in program order, so items stay in slot order
+        uint32_t prev = 0;
+        if (lane == leader) prev = atomicAdd(&S.warp_hist[w][dig], (uint32_t)__popc(peers));
+        rank[i] = __shfl_sync(0xffffffffu, prev, leader) + before;
     }
     __syncthreads();
     // thread d: exclusive prefix of digit d over warps, tile total

@@ -126,10 +126,10 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     float4* lcm = S.list_cm[w];
     uint32_t* lid = S.list_id[w];
 
-    const uint32_t bi = active ? b.idx_in[g] : 0u;
-    const float4 pm = b.leaf_pm[active ? g : grp.x];
+    const uint32_t bi0 = active ? b.idx_in[g] : 0u;
+    const float4 pm0 = b.leaf_pm[active ? g : grp.x];
     // group box (inactive lanes repeat the first body)
-    float mnx = pm.x, mny = pm.y, mnz = pm.z, mxx = pm.x, mxy = pm.y, mxz = pm.z;
+    float mnx = pm0.x, mny = pm0.y, mnz = pm0.z, mxx = pm0.x, mxy = pm0.y, mxz = pm0.z;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
@@ -147,7 +147,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     gg.R = sqrtf(hx * hx + hy * hy + hz * hz);
     gg.bmin = make_float3(mnx, mny, mnz);
     gg.bmax = make_float3(mxx, mxy, mxz);
-    gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi) : 0.0f;
+    gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi0) : 0.0f;
     if (MODE != GM_THETA) group_feature_terms(gg, G, soft);
     if (MODE == GM_LEARNED) {
         // the features read the group's terms from shared memory
@@ -157,10 +157,10 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     }
 
     // walk coordinates of this lane's body (absolute, or group-relative)
-    float4 pw = pm;
+    float4 pw = pm0;
     if (PREC) {
         const float4 lo_b = b.leaf_lo[active ? g : grp.x];
-        pw = make_float4((pm.x - gg.cx) + lo_b.x, (pm.y - gg.cy) + lo_b.y, (pm.z - gg.cz) + lo_b.z, pm.w);
+        pw = make_float4((pm0.x - gg.cx) + lo_b.x, (pm0.y - gg.cy) + lo_b.y, (pm0.z - gg.cz) + lo_b.z, pm0.w);
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
@@ -349,7 +349,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
                     // safe to accept (band_lo, default theta_g = 0.25) and one
                     // that must open (band_hi, default theta_g = 1): it never
                     // accepts a node the group reaches
-                    const float rho = group_rho(gg, ng);
+                    const float rho = group_rho(S.geom[w], ng);  // shared copy: fewer live registers
                     kind = rho < band_lo ? 1u : rho < band_hi ? 3u : 2u;
                 } else {
                     kind = group_theta_accept(gg, ng, theta) ? 1 : 2;
@@ -400,6 +400,9 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
         atomicAdd(&b.st->opened, (unsigned long long)opened);
     }
     if (active) {
+        // body index and position again (not kept live through the walk)
+        const uint32_t bi = b.idx_in[g];
+        const float4 pm = b.leaf_pm[g];
         if (PREC) {
             ax = ax + (nx_ - cx_);
             ay = ay + (ny_ - cy_);
