@@ -63,6 +63,7 @@ def workload(name: str, n: int | None):
             bodies=lambda: ic.plummer(n, seed=0),
             n=n,
             params=abi.step_params(dt=1e-3, theta=0.5, softening=0.01 ** 2, bounds=abi.BOUNDS_DYNAMIC),
+            plain_only=True,
         )
     if name == "uniform_merge":
         n = n or 1048576
@@ -73,6 +74,27 @@ def workload(name: str, n: int | None):
             params=abi.step_params(dt=5e-4, theta=0.7, softening=0.01 ** 2, mode=abi.MODE_MERGE,
                                    bounds=abi.BOUNDS_STATIC),
             bounds=np.array([-2, -2, -2, 2, 2, 2], np.float32),
+            plain_only=True,
+        )
+    if name == "clusters":
+        # 256 Gaussian clusters, power-law masses, merges on, learned criterion
+        n = n or 33554432
+        return dict(
+            name=f"cluster_mixture_n{n}",
+            bodies=lambda: ic.cluster_mixture(n, seed=4),
+            n=n,
+            params=abi.step_params(dt=1e-3, theta=0.5, softening=0.005 ** 2, mode=abi.MODE_MERGE,
+                                   bounds=abi.BOUNDS_DYNAMIC),
+        )
+    if name == "galaxy":
+        # two-galaxy encounter, precision form against the FP32 form
+        n = n or 8388608
+        return dict(
+            name=f"galaxy_pair_n{n}",
+            bodies=lambda: ic.galaxy_pair(n // 2, seed=2),
+            n=n,
+            params=abi.step_params(dt=1e-3, theta=0.5, softening=0.005 ** 2, bounds=abi.BOUNDS_DYNAMIC),
+            precision=True,
         )
     raise ValueError(name)
 
@@ -283,7 +305,7 @@ def run_reference(args):
     return 0
 
 
-LEARNED_TAUS = [-3.0, -2.75, -2.5, -2.25, -2.0, -1.75, -1.5]
+LEARNED_TAUS = [-3.0, -2.75, -2.6, -2.5, -2.4, -2.3, -2.2, -2.1, -2.0, -1.75, -1.5]
 GROUP_THETAS = [0.4, 0.45, 0.5, 0.55, 0.6, 0.65, 0.7]
 PLAIN_THETAS = [0.3, 0.5, 0.7]
 # DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +
@@ -319,6 +341,25 @@ def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
     return ms, st, clk
 
 
+def precision_arm(bh, p_plain, accuracy):
+    """The precision form (FP64 drift, compensated walk): its and the FP32
+    form's acceleration error against the FP64 direct sum on 4096 sampled
+    bodies of the current state, and the FP64 energy before the timed steps."""
+    p64 = abi.StepParams.from_buffer_copy(p_plain)
+    p64.precision_mode = abi.PRECISION_COMPENSATED
+    calib = {}
+    a64 = bh.evaluate_walk(p64)  # makes the FP64 positions current
+    live = accuracy.live_ids(bh)
+    sample = accuracy.sample_bodies(live, 4096, seed=2)
+    ref = bh.direct_sum(p64, sample)
+    err = lambda a: accuracy.summarize(np.linalg.norm(a[sample].astype(np.float64) - ref, axis=1) /
+                                       np.linalg.norm(ref, axis=1))
+    calib["compensated"] = err(a64)
+    calib["fp32"] = err(bh.evaluate_walk(p_plain))
+    calib["diagnostics_start"] = bh.diagnostics(p64)
+    return p64, calib
+
+
 def kernels_per_step(mac_mode: int) -> int:
     """Kernels of this library launched by one step (the CUDA graph's kernel
     nodes): reset 1, prepare 3, sort 1 + 8 passes, build 1, fill 2, walk 1
@@ -346,37 +387,48 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(bh.stream, device=f"cuda:{local}")
     soft = p_plain.softening
 
+    mode = p_plain.merging_collision_or_neither
+
     def learned(t):
         return abi.step_params(dt=p_plain.dt, theta=p_plain.theta, softening=soft, bounds=p_plain.static_or_dynamic,
-                               mac=abi.MAC_LEARNED, mac_tolerance=t)
+                               mac=abi.MAC_LEARNED, mac_tolerance=t, mode=mode)
 
     def group(t):
         return abi.step_params(dt=p_plain.dt, theta=t, softening=soft, bounds=p_plain.static_or_dynamic,
-                               mac=abi.MAC_GROUP)
+                               mac=abi.MAC_GROUP, mode=mode)
 
     def plain(t):
-        return abi.step_params(dt=p_plain.dt, theta=t, softening=soft, bounds=p_plain.static_or_dynamic)
+        return abi.step_params(dt=p_plain.dt, theta=t, softening=soft, bounds=p_plain.static_or_dynamic, mode=mode)
 
     # ---- learned criterion: train on this state, then pick the tolerance whose
     # p99 error stays at or below the plain theta = 0.5 walk's (untimed)
     calib = {}
     p_head = p_plain
     mac_name = "plain"
-    if not merging and not args.plain_only:
+    precision = bool(wl.get("precision"))
+    free0 = torch.cuda.mem_get_info(local)[0]
+    if precision:
+        p_head, calib = precision_arm(bh, p_plain, accuracy)
+        mac_name = "plain+compensated"
+    elif not (args.plain_only or wl.get("plain_only")):
         t0 = time.perf_counter()
         if args.mac_weights:
             bh.mac_set_weights(np.load(args.mac_weights))
             calib["weights"] = os.path.basename(args.mac_weights)
         else:
-            pairs = bh.mac_generate(p_plain, max_pairs=args.mac_pairs, seed=1)
+            p_grav = abi.StepParams.from_buffer_copy(p_plain)
+            p_grav.merging_collision_or_neither = abi.MODE_NEITHER  # the field only
+            pairs = bh.mac_generate(p_grav, max_pairs=args.mac_pairs, seed=1)
             losses = bh.mac_train(epochs=args.mac_epochs, batch=16384, lr=3e-3, seed=0)
             calib["training"] = {"pairs": pairs, "epochs": args.mac_epochs, "loss_first": float(losses[0]),
                                  "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
         judge = accuracy.Judge(bh, p_plain, count=4096, seed=2)
         ref = {th: accuracy.evaluate(bh, judge, plain(th)) for th in PLAIN_THETAS}
-        target = ref[p_plain.theta]["p99"] if p_plain.theta in ref else accuracy.evaluate(bh, judge, p_plain)["p99"]
-        calib["plain"] = {str(th): {k: r[k] for k in ("median", "p90", "p99", "max", "interactions")}
+        head = accuracy.evaluate(bh, judge, p_plain)
+        target = head["p99"]
+        calib["plain"] = {f"{th:g}": {k: r[k] for k in ("median", "p90", "p99", "max", "interactions")}
                           for th, r in ref.items()}
+        calib["plain_headline"] = {k: head[k] for k in ("median", "p90", "p99", "max", "interactions")}
         calib["p99_target"] = target
         if args.mac_tolerance is not None:
             tau = args.mac_tolerance
@@ -406,6 +458,10 @@ def run_ours(args):
     ms_step = ms_total / args.steps
     value = world * args.steps / (ms_total / 1000.0)
     interactions = int(st.interactions)
+    if precision:
+        calib["diagnostics_end"] = bh.diagnostics(p_head)
+        e0 = calib["diagnostics_start"]["total_energy"]
+        calib["relative_energy_change"] = (calib["diagnostics_end"]["total_energy"] - e0) / abs(e0)
 
     # per-stage times of the chosen walk (CUDA events between eager stage launches)
     prof = [bh.step_profiled(p_head) for _ in range(3)]
@@ -413,12 +469,19 @@ def run_ours(args):
     st_prof = bh.read_stats()
 
     # ---- comparison arms on the same context, same timing rules
+    footprint = free0 - torch.cuda.mem_get_info(local)[0]
     compare = {}
+    if precision and not args.no_compare:
+        ms_p, st_p, _ = timed_steps(bh, p_plain, args.steps, args.warmup, stream, dist, local)
+        compare["fp32_form"] = {"steps_per_s": world * args.steps / (ms_p / 1000.0), "ms_per_step": ms_p / args.steps,
+                                "p99": calib["fp32"]["p99"]}
+        compare["compensated_form"] = {"steps_per_s": value, "ms_per_step": ms_step,
+                                       "p99": calib["compensated"]["p99"]}
     if mac_name == "learned" and not args.no_compare:
         ms_p, st_p, clk_p = timed_steps(bh, p_plain, args.steps, args.warmup, stream, dist, local,
                                         ClockSampler(local))
         compare["plain_theta"] = {"theta": p_plain.theta, "steps_per_s": world * args.steps / (ms_p / 1000.0),
-                                  "ms_per_step": ms_p / args.steps, "p99": calib["plain"][str(p_plain.theta)]["p99"],
+                                  "ms_per_step": ms_p / args.steps, "p99": calib["plain_headline"]["p99"],
                                   "interactions_per_step": int(st_p.interactions), "clocks": clk_p}
         compare["learned"] = {"mac_tolerance": calib["learned"]["mac_tolerance"], "steps_per_s": value,
                               "ms_per_step": ms_step, "p99": calib["learned"]["p99"],
@@ -502,6 +565,7 @@ def run_ours(args):
             "n_bodies": wl["n"],
             "softening": soft,
             "mac": mac_name,
+            "merges": bool(merging),
             "mac_tolerance": calib.get("learned", {}).get("mac_tolerance"),
             "plain_theta": p_plain.theta,
             "l2": "inputs larger than L2 (bodies 537 MB, tree + sort buffers ~5 GB)",
@@ -514,7 +578,8 @@ def run_ours(args):
         "calibration": calib,
         "stage_ms": stage_ms,
         "roofline": {
-            "kernel": "k_walk_group<learned>" if mac_name == "learned" else "k_walk_plain",
+            "kernel": {"learned": "k_walk_group<learned>", "plain+compensated": "k_walk_plain<compensated>"}.get(
+                mac_name, "k_walk_plain"),
             "bound": "fp32",
             "achieved": achieved,
             "peak": fp32_peak,
@@ -539,6 +604,7 @@ def run_ours(args):
         "e2e": e2e,
         "clocks": clk,
         "stats": abi.stats_to_dict(st),
+        "footprint_bytes": int(footprint),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -550,7 +616,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mixture", choices=["mixture", "plummer", "uniform_merge"])
+    ap.add_argument("--workload", default="mixture",
+                    choices=["mixture", "plummer", "uniform_merge", "clusters", "galaxy"])
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)

@@ -204,8 +204,8 @@ static int upload_params(gbh_ctx* c, const gbh_step_params* p) {
     if ((p->flags & GBH_FLAG_STORE_ACCEL) && !c->accel) return fail(c, GBH_ERR_INVALID, "accel buffer missing");
     if (p->mac_mode == GBH_MAC_LEARNED && !c->mac_ready)
         return fail(c, GBH_ERR_STATE, "learned MAC selected but no weights were set");
-    if (p->mac_mode != GBH_MAC_PLAIN && p->merging_collision_or_neither != GBH_MODE_NEITHER)
-        return fail(c, GBH_ERR_UNSUPPORTED, "group and learned acceptance criteria run gravity only (no merges or collisions)");
+    if (p->mac_mode != GBH_MAC_PLAIN && p->merging_collision_or_neither == GBH_MODE_COLLISION)
+        return fail(c, GBH_ERR_UNSUPPORTED, "group and learned acceptance criteria run gravity and merges (no collisions)");
     if (p->precision_mode == GBH_PRECISION_COMPENSATED && p->merging_collision_or_neither != GBH_MODE_NEITHER)
         return fail(c, GBH_ERR_UNSUPPORTED, "the precision form runs gravity only (no merges or collisions)");
     if (p->precision_mode == GBH_PRECISION_COMPENSATED || (p->flags & GBH_FLAG_STORE_POTENTIAL)) {

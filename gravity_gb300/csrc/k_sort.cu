@@ -8,8 +8,9 @@
 // Merrill 2022): 8 passes of 8-bit digits, one kernel per pass.
 //   * The eight digit histograms are accumulated by the encode pass
 //     (k_prep_scatter) and scanned here once (k_sort_scan).
-//   * Each pass kernel takes a tile ticket, ranks its keys with warp
-//     match-any, publishes the tile's digit counts, resolves its global digit
+//   * Each pass kernel takes a tile ticket, ranks its keys per warp (digit
+//     peers from one ballot per digit bit, ranks reserved with shared-memory
+//     atomics in item order), publishes the tile's digit counts, resolves its global digit
 //     offsets with a decoupled look-back (bounded spin, error word on
 //     timeout), stages keys digit-ordered in shared memory and writes them out
 //     with coalesced runs.
@@ -88,7 +89,15 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, ui
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t pos = seg + i * 32 + lane;
         const uint32_t dig = pos < n ? (uint32_t)((key[i] >> shift) & 0xFF) : SORT_RADIX;
-        const uint32_t peers = __match_any_sync(0xffffffffu, dig);
+        // lanes with the same digit (9 bits: 256 is the sentinel of
+        // out-of-range slots), from one ballot per bit
+        uint32_t peers = 0xffffffffu;
+#pragma unroll
+        for (int bit = 0; bit < 9; ++bit) {
+            const bool on = (dig >> bit) & 1u;
+            const uint32_t m = __ballot_sync(0xffffffffu, on);
+            peers &= on ? m : ~m;
+        }
         const uint32_t leader = __ffs(peers) - 1;
         const uint32_t before = __popc(peers & lanemask_lt());
         // the digit's leader reserves the group's ranks; a warp's shared

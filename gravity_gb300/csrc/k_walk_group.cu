@@ -76,24 +76,36 @@ __global__ void k_find_groups(StepBuffers b) {
         }
         return;
     }
+    // an internal node t and a leaf t can each start a group
+    uint2 mine[2];
+    uint32_t k = 0;
     if (t + 1 < n) {
         const gbh_node* nd = &b.internal[t];
         const uint32_t cnt = nd->bodies_contained;
         if (cnt <= GBH_GROUP_MAX) {
             const uint32_t p = nd->parent_id;
-            if (p == GBH_NONE || b.internal[p - N].bodies_contained > GBH_GROUP_MAX) {
-                const uint32_t slot = atomicAdd(&b.st->num_groups, 1u);
-                b.groups[slot] = make_uint2(b.node_lo[t], cnt);
-            }
+            if (p == GBH_NONE || b.internal[p - N].bodies_contained > GBH_GROUP_MAX)
+                mine[k++] = make_uint2(b.node_lo[t], cnt);
         }
     }
     if (t < n) {
         const uint32_t p = b.leaf[t].parent_id;
-        if (p != GBH_NONE && b.internal[p - N].bodies_contained > GBH_GROUP_MAX) {
-            const uint32_t slot = atomicAdd(&b.st->num_groups, 1u);
-            b.groups[slot] = make_uint2(t, 1u);
-        }
+        if (p != GBH_NONE && b.internal[p - N].bodies_contained > GBH_GROUP_MAX) mine[k++] = make_uint2(t, 1u);
     }
+    // one counter update per warp (a single global counter would serialise)
+    const uint32_t lane = lane_id();
+    uint32_t incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&b.st->num_groups, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    const uint32_t first = base + incl - k;
+    for (uint32_t q = 0; q < k; ++q) b.groups[first + q] = mine[q];
 }
 
 // PREC: the precision form.  The lanes' bodies and the list entries are kept
@@ -163,6 +175,10 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
         pw = make_float4((pm0.x - gg.cx) + lo_b.x, (pm0.y - gg.cy) + lo_b.y, (pm0.z - gg.cz) + lo_b.z, pm0.w);
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
+    // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
+    const bool merging = !PREC && P->merging_collision_or_neither == GBH_MODE_MERGE;
+    const float my_rad = (merging && active) ? b.leaf_rad[g] : 0.0f;
+    uint32_t seq = 0;
     float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
     float nx_ = 0.f, ny_ = 0.f, nz_ = 0.f, np_ = 0.f;  // PREC: leaf terms (Kahan)
     float cx_ = 0.f, cy_ = 0.f, cz_ = 0.f, cp_ = 0.f;
@@ -177,13 +193,30 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
     const bool self_check = !(soft >= 1e-20f);
     auto flush = [&](uint32_t cnt) {
-        if (PREC || want_pot) {
-            // the general loop: leaf terms apart (PREC), potential, self check
+        if (PREC || want_pot || merging) {
+            // the general loop: leaf terms apart (PREC), potential, self
+            // check, merge tasks
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
                 const uint32_t lj = lid[j];
                 const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
+                if (merging && lj < N && active && lj != g) {
+                    // penetration with the leaf's body; a task when positive
+                    // and this body's index is the smaller
+                    const float pen = my_rad + b.leaf_rad[lj] - sqrtf(rx * rx + ry * ry + rz * rz);
+                    if (pen > 0.0f) {
+                        const uint32_t bi = b.idx_in[g], oi = b.idx_in[lj];
+                        if (bi < oi) {
+                            const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
+                            if (slot < N) {
+                                b.mq->pairs[slot] = make_uint2(bi, oi);
+                                b.mkeys[slot] = ((unsigned long long)g << 32) | seq;
+                            }
+                            ++seq;
+                        }
+                    }
+                }
                 const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                 const float inv = rsqrtf(rr);
                 const bool self = self_check && lj == g;

@@ -117,3 +117,48 @@ def test_learned_mac_pipeline_and_gain(gbh_lib):
         [0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.2], target)
     assert best_l is not None and best_g is not None, (res_l, res_g)
     assert best_l[1]["interactions"] < best_g[1]["interactions"], (best_l, best_g)
+
+
+def test_group_and_learned_walks_emit_merge_tasks(gbh_lib):
+    # dense uniform cube with merge radii: every task the group walk emits is
+    # a genuinely overlapping pair (body index first smaller), it finds the
+    # plain walk's tasks, and merge resolution conserves mass
+    n = 20000
+    b = ic.uniform_merge(n, seed=1)
+    b["pos_mass"][:, :3] *= 0.1
+    bounds = np.array([-2, -2, -2, 2, 2, 2], np.float32)
+    kw = dict(dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+
+    def tasks(params):
+        sim = BarnesHut(n, bounds, abi.units(G=1.0))
+        sim.upload_bodies(b)
+        sim.init()
+        sim.reset_values(params)
+        sim.partition_dead_bodies(params)
+        sim.radix_sort()
+        sim.build_binary_radix_tree()
+        sim.compute_com_and_location()
+        sim.compute_force(params)
+        return sim, sim.read_merge_tasks()
+
+    _, t_plain = tasks(abi.step_params(**kw))
+    sim, t_group = tasks(abi.step_params(mac=abi.MAC_GROUP, **kw))
+    assert len(t_plain) > 100
+    pos = b["pos_mass"][:, :3].astype(np.float64)
+    rad = 0.6203504909 * (b["pos_mass"][:, 3].astype(np.float64) / ic.MERGE_DENSITY) ** (1.0 / 3.0)
+    i, j = t_group[:, 0].astype(np.int64), t_group[:, 1].astype(np.int64)
+    assert np.all(i < j)
+    assert np.all(np.linalg.norm(pos[i] - pos[j], axis=1) < (rad[i] + rad[j]) * (1 + 1e-5))
+    sp, sg = set(map(tuple, t_plain.tolist())), set(map(tuple, t_group.tolist()))
+    assert len(sp & sg) >= 0.99 * len(sp)
+    m0 = sim.read_bodies()["pos_mass"][:, 3].astype(np.float64).sum()
+    sim.merge_bodies(abi.step_params(mac=abi.MAC_GROUP, **kw))
+    assert sim.read_stats().merged > 0
+    m1 = sim.read_bodies(abi.BODIES_OUT)["pos_mass"][:, 3].astype(np.float64).sum()
+    assert m1 == pytest.approx(m0, rel=1e-5)
+    # the learned walk runs with merges too
+    rng = np.random.default_rng(0)
+    sim.mac_set_weights(rng.normal(0, 0.1, abi.MAC_NUM_PARAMS).astype(np.float32))
+    sim.step(abi.step_params(mac=abi.MAC_LEARNED, mac_tolerance=-2.0, **kw), count=2)
+    sim.synchronize()
+    assert sim.read_stats().error_word == 0
