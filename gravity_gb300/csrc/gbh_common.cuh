@@ -108,6 +108,7 @@ struct StepBuffers {
     float4* leaf_lo;         // by sorted slot: FP32 residual x64 - (float)x64 of the leaf's body
     float* potential;        // walk potential by body id (GBH_FLAG_STORE_POTENTIAL)
     uint32_t prec;           // 1: this step runs the precision form
+    uint32_t merge;          // 1: this step emits merge tasks (mode GBH_MODE_MERGE)
     // compaction scratch
     uint32_t* tile_dead;
     float* tile_aabb;

@@ -84,6 +84,7 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.leaf_lo = c->leaf_lo;
     b.potential = c->potential;
     b.prec = (c->params_valid && c->params_host.precision_mode == GBH_PRECISION_COMPENSATED && c->pos64[0]) ? 1u : 0u;
+    b.merge = (c->params_valid && c->params_host.merging_collision_or_neither == GBH_MODE_MERGE) ? 1u : 0u;
     b.tile_dead = c->tile_dead;
     b.tile_aabb = c->tile_aabb;
     b.hist = c->hist;
@@ -377,7 +378,8 @@ int gbh_init(gbh_ctx* c) {
 
 static int graph_key(const gbh_ctx* c) {
     return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2) |
-           ((c->params_host.precision_mode == GBH_PRECISION_COMPENSATED) ? 16 : 0);
+           ((c->params_host.precision_mode == GBH_PRECISION_COMPENSATED) ? 16 : 0) |
+           ((int)c->params_host.merging_collision_or_neither << 5);
 }
 
 int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1); }

@@ -11,7 +11,8 @@
 //     list on their own body (dense FMA loop, node data broadcast from shared
 //     memory).
 // Criteria (gbh_step_params.mac_mode):
-//   GBH_MAC_GROUP    accept when half_side < theta * (|com - c_g| - R_g), with
+//   GBH_MAC_GROUP    accept when the boxes are disjoint and half_side < theta *
+//                    sqrt(d^2 + softening), d = max(|com - c_g| - R_g, 0), with
 //                    c_g, R_g the centre and half diagonal of the group's box;
 //   GBH_MAC_LEARNED  nodes that pass the group rule at the band's lower theta
 //                    (default 0.25) are accepted, nodes that fail it at its
@@ -112,9 +113,15 @@ __global__ void k_find_groups(StepBuffers b) {
 // relative to the group centre c_g: (x - c_g) + lo for a leaf (lo its FP32
 // residual), com - c_g for a node; leaf terms are summed with Kahan
 // compensation apart from the node terms.
-template <int MODE, bool PREC>
-__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) void k_walk_group(StepBuffers b,
-                                                                                             MacDeviceWeights mw) {
+// FORM: the arithmetic form and the step's extra work, fixed per instance so
+// that the common case keeps its registers: FORM_FP32, FORM_PREC (precision
+// form), FORM_MERGE (merge tasks from the leaf entries).
+enum GroupForm { FORM_FP32 = 0, FORM_PREC = 1, FORM_MERGE = 2 };
+
+template <int MODE, int FORM>
+__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32) ? 4 : 3) void k_walk_group(
+    StepBuffers b, MacDeviceWeights mw) {
+    constexpr bool PREC = FORM == FORM_PREC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Cfg = GroupCfg<MODE>;
     typename Cfg::Smem& S = *reinterpret_cast<typename Cfg::Smem*>(smem_raw);
@@ -160,6 +167,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     gg.bmin = make_float3(mnx, mny, mnz);
     gg.bmax = make_float3(mxx, mxy, mxz);
     gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi0) : 0.0f;
+    gg.soft = soft;
     if (MODE != GM_THETA) group_feature_terms(gg, G, soft);
     if (MODE == GM_LEARNED) {
         // the features read the group's terms from shared memory
@@ -176,7 +184,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && !PREC) ? 4 : 3) vo
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
-    const bool merging = !PREC && P->merging_collision_or_neither == GBH_MODE_MERGE;
+    constexpr bool merging = FORM == FORM_MERGE;
     const float my_rad = (merging && active) ? b.leaf_rad[g] : 0.0f;
     uint32_t seq = 0;
     float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
@@ -460,17 +468,19 @@ static size_t group_smem(int mode) {
                                                                               : GroupCfg<GM_THETA>::smem;
 }
 
-template <int MODE, bool PREC>
+template <int MODE, int FORM>
 static void set_smem() {
-    cudaFuncSetAttribute(k_walk_group<MODE, PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(MODE));
+    cudaFuncSetAttribute(k_walk_group<MODE, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(MODE));
 }
 
 void group_walk_setup() {
-    set_smem<GM_THETA, false>();
-    set_smem<GM_THETA, true>();
-    set_smem<GM_LEARNED, false>();
-    set_smem<GM_LEARNED, true>();
-    set_smem<GM_RECORD, false>();
+    set_smem<GM_THETA, FORM_FP32>();
+    set_smem<GM_THETA, FORM_PREC>();
+    set_smem<GM_THETA, FORM_MERGE>();
+    set_smem<GM_LEARNED, FORM_FP32>();
+    set_smem<GM_LEARNED, FORM_PREC>();
+    set_smem<GM_LEARNED, FORM_MERGE>();
+    set_smem<GM_RECORD, FORM_FP32>();
 }
 
 void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
@@ -478,28 +488,31 @@ void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
     k_find_groups<<<(b.N + 255) / 256, 256, 0, s>>>(b);
 }
 
-template <int MODE, bool PREC>
+template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
     if (MODE != GM_RECORD) launch_find_groups(b, s);
     const uint32_t blocks = (b.N + GW_THREADS - 1) / GW_THREADS;
-    k_walk_group<MODE, PREC><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
+    k_walk_group<MODE, FORM><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
+}
+
+template <int MODE>
+static void launch_form(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
+    if (b.prec)
+        launch_mode<MODE, FORM_PREC>(b, mw, s);
+    else if (b.merge)
+        launch_mode<MODE, FORM_MERGE>(b, mw, s);
+    else
+        launch_mode<MODE, FORM_FP32>(b, mw, s);
 }
 
 void launch_walk_group(const StepBuffers& b, const MacDeviceWeights& mw, bool learned, cudaStream_t s) {
-    if (learned) {
-        if (b.prec)
-            launch_mode<GM_LEARNED, true>(b, mw, s);
-        else
-            launch_mode<GM_LEARNED, false>(b, mw, s);
-    } else {
-        if (b.prec)
-            launch_mode<GM_THETA, true>(b, mw, s);
-        else
-            launch_mode<GM_THETA, false>(b, mw, s);
-    }
+    if (learned)
+        launch_form<GM_LEARNED>(b, mw, s);
+    else
+        launch_form<GM_THETA>(b, mw, s);
 }
 
 // the caller runs launch_find_groups once first: pairs name groups by index
 void launch_walk_group_record(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
-    launch_mode<GM_RECORD, false>(b, mw, s);
+    launch_mode<GM_RECORD, FORM_FP32>(b, mw, s);
 }

@@ -104,30 +104,36 @@ __device__ __forceinline__ float box_gap2(const GroupGeom& g, const NodeGeom& n)
     return gx * gx + gy * gy + gz * gz;
 }
 
-// Group theta rule (the learned criterion's ablation): accept when the boxes
-// of the group and the node are disjoint and the node's half side is below
-// theta times the distance D from its centre of mass to the group's bounding
-// sphere, half < theta (D - R), evaluated without a square root as
-// (half + theta R)^2 < theta^2 D^2 (theta > 0).
-__device__ __forceinline__ bool group_theta_accept(const GroupGeom& g, const NodeGeom& n, float theta) {
-    const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
-    const float half = 0.5f * fmaxf(ex, fmaxf(ey, ez));
+// Group theta rule (the learned criterion's ablation), with the softened
+// distance of the reference's rule (bh_force.comp:62-66 adds the softening to
+// r.r): accept when the boxes of the group and the node are disjoint and the
+// node's half side is below theta times sqrt(d^2 + softening), d the distance
+// from its centre of mass to the group's bounding sphere (0 inside it).
+__device__ __forceinline__ float group_soft_dist2(const GroupGeom& g, const NodeGeom& n) {
     const float dx = n.cm.x - g.cx, dy = n.cm.y - g.cy, dz = n.cm.z - g.cz;
     const float D2 = dx * dx + dy * dy + dz * dz;
-    const float t = half + theta * g.R;
-    return theta > 0.0f && t * t < theta * theta * D2 && box_gap2(g, n) > 0.0f;
+    const float D = D2 > 0.0f ? D2 * rsqrtf(D2) : 0.0f;
+    const float d = fmaxf(D - g.R, 0.0f);
+    return d * d + g.soft;
+}
+
+__device__ __forceinline__ float node_half(const NodeGeom& n) {
+    const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
+    return 0.5f * fmaxf(ex, fmaxf(ey, ez));
+}
+
+__device__ __forceinline__ bool group_theta_accept(const GroupGeom& g, const NodeGeom& n, float theta) {
+    const float half = node_half(n);
+    return theta > 0.0f && half * half < theta * theta * group_soft_dist2(g, n) && box_gap2(g, n) > 0.0f;
 }
 
 // The smallest theta at which the group rule accepts the node,
-// rho = half / (D - R); +inf when the boxes overlap or the centre of mass lies
-// inside the group's bounding sphere.  The learned walk and the recording of
-// training pairs compare it against the band's two thetas.
+// rho = half / sqrt(d^2 + softening); +inf when the boxes overlap.  The
+// learned walk and the recording of training pairs compare it against the
+// band's two thetas.
 __device__ __forceinline__ float group_rho(const GroupGeom& g, const NodeGeom& n) {
-    const float ex = n.bmax.x - n.bmin.x, ey = n.bmax.y - n.bmin.y, ez = n.bmax.z - n.bmin.z;
-    const float half = 0.5f * fmaxf(ex, fmaxf(ey, ez));
-    const float dx = n.cm.x - g.cx, dy = n.cm.y - g.cy, dz = n.cm.z - g.cz;
-    const float den = sqrtf(dx * dx + dy * dy + dz * dz) - g.R;
-    return (den > 0.0f && box_gap2(g, n) > 0.0f) ? __fdividef(half, den) : __int_as_float(0x7f800000);
+    const float den2 = group_soft_dist2(g, n);
+    return (den2 > 0.0f && box_gap2(g, n) > 0.0f) ? node_half(n) * rsqrtf(den2) : __int_as_float(0x7f800000);
 }
 
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
