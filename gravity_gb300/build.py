@@ -4,6 +4,9 @@ Every .cu file under csrc/ is compiled in parallel by nvcc into
 gravity_gb300/_build/ and linked into gravity_gb300/libgbh.so.  The library is
 compiled with --fmad=false: the step's FP32 arithmetic rounds once per
 operation, in source order, like the reference GLSL restated as IEEE FP32.
+The group and learned walks (k_walk_group.cu) are new algorithms with no
+bit-level counterpart in the reference, so their translation unit lets the
+compiler contract multiply-adds.
 """
 from __future__ import annotations
 
@@ -19,8 +22,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbh.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
                 "-I", os.path.join(HERE, "..", "include")]
+FMAD_CONTRACT = {"k_walk_group.cu"}
 
 
 def _compile(src: str) -> str:
@@ -29,7 +33,8 @@ def _compile(src: str) -> str:
     deps.append(os.path.join(HERE, "..", "include", "gbh.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [NVCC] + FLAGS + ["-c", src, "-o", obj]
+    fmad = "--fmad=true" if os.path.basename(src) in FMAD_CONTRACT else "--fmad=false"
+    cmd = [NVCC] + FLAGS + [fmad, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

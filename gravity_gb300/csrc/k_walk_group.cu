@@ -65,7 +65,10 @@ struct GroupCfg {
 
 // Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
 // more (every leaf lies in exactly one).  A group is a contiguous range of
-// sorted slots, spatially compact because it is one tree node.
+// sorted slots, spatially compact because it is one tree node.  Found from the
+// parent side: each internal node with more than GBH_GROUP_MAX bodies emits
+// its children that hold at most that many (the children's counts are read
+// only for the large nodes).
 __global__ void k_find_groups(StepBuffers b) {
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
@@ -77,23 +80,30 @@ __global__ void k_find_groups(StepBuffers b) {
         }
         return;
     }
-    // an internal node t and a leaf t can each start a group
     uint2 mine[2];
     uint32_t k = 0;
     if (t + 1 < n) {
-        const gbh_node* nd = &b.internal[t];
-        const uint32_t cnt = nd->bodies_contained;
-        if (cnt <= GBH_GROUP_MAX) {
-            const uint32_t p = nd->parent_id;
-            if (p == GBH_NONE || b.internal[p - N].bodies_contained > GBH_GROUP_MAX)
-                mine[k++] = make_uint2(b.node_lo[t], cnt);
+        // childA, childB (Node words @40, @44) and bodiesContained (@52); the
+        // node is 80 bytes, so these are 8-byte aligned pairs
+        const uint2 kids = __ldg(reinterpret_cast<const uint2*>(&b.internal[t].child_a));
+        const uint32_t cnt = __ldg(&b.internal[t].bodies_contained);
+        const uint2 w = kids;
+        if (cnt > GBH_GROUP_MAX) {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const uint32_t ch = c == 0 ? w.x : w.y;
+                if (ch < N) {
+                    mine[k++] = make_uint2(ch, 1u);
+                } else {
+                    const uint32_t cc = __ldg(&b.internal[ch - N].bodies_contained);
+                    if (cc <= GBH_GROUP_MAX) mine[k++] = make_uint2(__ldg(&b.node_lo[ch - N]), cc);
+                }
+            }
+        } else if (t == 0) {
+            mine[k++] = make_uint2(0u, cnt);  // the whole tree is one group
         }
     }
-    if (t < n) {
-        const uint32_t p = b.leaf[t].parent_id;
-        if (p != GBH_NONE && b.internal[p - N].bodies_contained > GBH_GROUP_MAX) mine[k++] = make_uint2(t, 1u);
-    }
-    // one counter update per warp (a single global counter would serialise)
+    // one counter update per warp
     const uint32_t lane = lane_id();
     uint32_t incl = k;
 #pragma unroll
