@@ -112,29 +112,21 @@ __global__ void k_mac_predict(const float* __restrict__ feats, uint32_t n, float
 
 // ---------------------------------------------------------------------------
 // labels of recorded pairs: one warp per pair
-__global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, const uint32_t* __restrict__ count,
-                            float* __restrict__ labels) {
-    const uint32_t lane = lane_id();
-    const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t np = *count;
-    if (p >= np) return;
+// Relative error of the node's monopole against its exact subtree sum on the
+// body in sorted slot g (accelerations of the last reference walk in b.accel).
+__device__ float mac_label_body(const StepBuffers& b, uint32_t node, uint32_t g) {
     const uint32_t N = b.N;
-    const uint2 pr = pairs[p];
-    const uint2 grp = b.groups[pr.x];
-    const uint32_t g = grp.x + lane;
-    const bool active = lane < grp.y;
     const float G = b.sim->gravitational_constant;
     const float soft = b.params->softening;
-    const float4 pm = b.leaf_pm[active ? g : grp.x];
-    const uint32_t bi = active ? b.idx_in[g] : 0u;
-    const gbh_node* nd = &b.internal[pr.y - N];
+    const float4 pm = b.leaf_pm[g];
+    const gbh_node* nd = &b.internal[node - N];
     const float4 cm = *reinterpret_cast<const float4*>(nd);
     const uint32_t cnt = nd->bodies_contained;
     float ex = 0.f, ey = 0.f, ez = 0.f;
     if (cnt <= MAC_LABEL_MAX_BODIES) {
         // exact: every body of the subtree (its contiguous sorted range, which
         // starts at the subtree's leftmost leaf)
-        uint32_t id = pr.y;
+        uint32_t id = node;
         while (id >= N) id = b.internal[id - N].child_a;
         const uint32_t lo = id;
         for (uint32_t j = lo; j < lo + cnt; ++j) {
@@ -152,7 +144,7 @@ __global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, cons
         // the half side), accurate to ~1e-5 of the subtree's pull
         uint32_t stack[MAC_LABEL_STACK];
         uint32_t sp = 0;
-        stack[sp++] = pr.y;
+        stack[sp++] = node;
         while (sp > 0) {
             const uint32_t id = stack[--sp];
             if (id < N) {
@@ -191,12 +183,23 @@ __global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, cons
     const float inv = rsqrtf(rx * rx + ry * ry + rz * rz + soft);
     const float f = G * cm.w * inv * inv * inv;
     const float dx = f * rx - ex, dy = f * ry - ey, dz = f * rz - ez;
+    const float4 a = b.accel[b.idx_in[g]];
+    const float amag = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+    return sqrtf(dx * dx + dy * dy + dz * dz) / fmaxf(amag, 1e-30f);
+}
+
+// One warp per pair: lane l takes the group's bodies l, l + 32, ...; the label
+// is log10 of the largest error over the group.
+__global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, const uint32_t* __restrict__ count,
+                            float* __restrict__ labels) {
+    const uint32_t lane = lane_id();
+    const uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t np = *count;
+    if (p >= np) return;
+    const uint2 pr = pairs[p];
+    const uint2 grp = b.groups[pr.x];
     float err = 0.0f;
-    if (active) {
-        const float4 a = b.accel[bi];
-        const float amag = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
-        err = sqrtf(dx * dx + dy * dy + dz * dz) / fmaxf(amag, 1e-30f);
-    }
+    for (uint32_t k = lane; k < grp.y; k += 32) err = fmaxf(err, mac_label_body(b, pr.y, grp.x + k));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) err = fmaxf(err, __shfl_xor_sync(0xffffffffu, err, o));
     if (lane == 0) labels[p] = log10f(fmaxf(err, 1e-12f));

@@ -1,15 +1,15 @@
-// k_walk_group.cu — group walk: one acceptance decision per (32-body group, node).
+// k_walk_group.cu — group walk: one acceptance decision per (body group, node).
 //
 // The reference decides per body (bh_force.comp:57-115).  Here a warp takes
-// one body group, a subtree of at most 32 bodies (k_find_groups), and walks
-// the tree once for all of its bodies:
+// one body group, a subtree of at most GBH_GROUP_MAX = 64 bodies (two per
+// lane; k_find_groups), and walks the tree once for all of its bodies:
 //   * candidates come off a per-warp stack 32 at a time, one per lane; each
 //     lane evaluates the acceptance criterion of the group against its node;
 //   * accepted nodes and leaves are appended to an interaction list, opened
 //     nodes push their two children;
-//   * every 32 list entries, all 32 lanes accumulate the forces of the whole
-//     list on their own body (dense FMA loop, node data broadcast from shared
-//     memory).
+//   * every 32 list entries, all lanes accumulate the forces of the whole
+//     list on their own bodies (dense FMA loop, node data broadcast from
+//     shared memory).
 // Criteria (gbh_step_params.mac_mode):
 //   GBH_MAC_GROUP    accept when the boxes are disjoint and half_side < theta *
 //                    sqrt(d^2 + softening), d = max(|com - c_g| - R_g, 0), with
@@ -34,6 +34,7 @@
 #define GW_STACK 768
 #define GW_LIST 64
 #define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
+#define GW_BPL (GBH_GROUP_MAX / 32)  // bodies per lane
 
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 
@@ -129,7 +130,7 @@ __global__ void k_find_groups(StepBuffers b) {
 enum GroupForm { FORM_FP32 = 0, FORM_PREC = 1, FORM_MERGE = 2 };
 
 template <int MODE, int FORM>
-__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32) ? 4 : 3) void k_walk_group(
+__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32) ? 3 : 2) void k_walk_group(
     StepBuffers b, MacDeviceWeights mw) {
     constexpr bool PREC = FORM == FORM_PREC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -142,11 +143,17 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     const uint32_t N = b.N;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t num_groups = b.st->num_groups;
-    // groups hold up to 32 bodies, usually fewer: warps loop over them
+    // groups hold up to GBH_GROUP_MAX bodies, usually fewer: warps loop over
+    // them; lane l holds bodies l and l + 32 of the group
     for (uint32_t gi = blockIdx.x * GW_WARPS + w; gi < num_groups; gi += gridDim.x * GW_WARPS) {
     const uint2 grp = b.groups[gi];
-    const uint32_t g = grp.x + lane;
-    const bool active = lane < grp.y;
+    uint32_t gq[GW_BPL];
+    bool actq[GW_BPL];
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) {
+        gq[q] = grp.x + lane + 32u * q;
+        actq[q] = lane + 32u * q < grp.y;
+    }
     const gbh_step_params* P = b.params;
     const gbh_sim_values* sim = b.sim;
     const float G = sim->gravitational_constant;
@@ -155,10 +162,20 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     float4* lcm = S.list_cm[w];
     uint32_t* lid = S.list_id[w];
 
-    const uint32_t bi0 = active ? b.idx_in[g] : 0u;
-    const float4 pm0 = b.leaf_pm[active ? g : grp.x];
-    // group box (inactive lanes repeat the first body)
-    float mnx = pm0.x, mny = pm0.y, mnz = pm0.z, mxx = pm0.x, mxy = pm0.y, mxz = pm0.z;
+    // group box (inactive slots repeat the first body)
+    float4 pmq[GW_BPL];
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) pmq[q] = b.leaf_pm[actq[q] ? gq[q] : grp.x];
+    float mnx = pmq[0].x, mny = pmq[0].y, mnz = pmq[0].z, mxx = pmq[0].x, mxy = pmq[0].y, mxz = pmq[0].z;
+#pragma unroll
+    for (int q = 1; q < GW_BPL; ++q) {
+        mnx = fminf(mnx, pmq[q].x);
+        mny = fminf(mny, pmq[q].y);
+        mnz = fminf(mnz, pmq[q].z);
+        mxx = fmaxf(mxx, pmq[q].x);
+        mxy = fmaxf(mxy, pmq[q].y);
+        mxz = fmaxf(mxz, pmq[q].z);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
@@ -176,7 +193,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     gg.R = sqrtf(hx * hx + hy * hy + hz * hz);
     gg.bmin = make_float3(mnx, mny, mnz);
     gg.bmax = make_float3(mxx, mxy, mxz);
-    gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, active, bi0) : 0.0f;
+    gg.a_ref = (MODE != GM_THETA) ? group_accel_ref(b, actq, gq) : 0.0f;
     gg.soft = soft;
     if (MODE != GM_THETA) group_feature_terms(gg, G, soft);
     if (MODE == GM_LEARNED) {
@@ -186,20 +203,35 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         __syncwarp();
     }
 
-    // walk coordinates of this lane's body (absolute, or group-relative)
-    float4 pw = pm0;
-    if (PREC) {
-        const float4 lo_b = b.leaf_lo[active ? g : grp.x];
-        pw = make_float4((pm0.x - gg.cx) + lo_b.x, (pm0.y - gg.cy) + lo_b.y, (pm0.z - gg.cz) + lo_b.z, pm0.w);
+    // walk coordinates of this lane's bodies (absolute, or group-relative)
+    float3 pw[GW_BPL];
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) {
+        pw[q] = make_float3(pmq[q].x, pmq[q].y, pmq[q].z);
+        if (PREC) {
+            const float4 lo_b = b.leaf_lo[actq[q] ? gq[q] : grp.x];
+            pw[q] = make_float3((pmq[q].x - gg.cx) + lo_b.x, (pmq[q].y - gg.cy) + lo_b.y, (pmq[q].z - gg.cz) + lo_b.z);
+        }
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
     constexpr bool merging = FORM == FORM_MERGE;
-    const float my_rad = (merging && active) ? b.leaf_rad[g] : 0.0f;
-    uint32_t seq = 0;
-    float ax = 0.f, ay = 0.f, az = 0.f, pot = 0.f;
-    float nx_ = 0.f, ny_ = 0.f, nz_ = 0.f, np_ = 0.f;  // PREC: leaf terms (Kahan)
-    float cx_ = 0.f, cy_ = 0.f, cz_ = 0.f, cp_ = 0.f;
+    float my_rad[GW_BPL];
+    uint32_t seq[GW_BPL];
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) {
+        my_rad[q] = (merging && actq[q]) ? b.leaf_rad[gq[q]] : 0.0f;
+        seq[q] = 0;
+    }
+    float ax[GW_BPL], ay[GW_BPL], az[GW_BPL], pot[GW_BPL];
+    float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], np_[GW_BPL];  // PREC: leaf terms (Kahan)
+    float cx_[GW_BPL], cy_[GW_BPL], cz_[GW_BPL], cp_[GW_BPL];
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) {
+        ax[q] = ay[q] = az[q] = pot[q] = 0.f;
+        nx_[q] = ny_[q] = nz_[q] = np_[q] = 0.f;
+        cx_[q] = cy_[q] = cz_[q] = cp_[q] = 0.f;
+    }
     uint32_t inter = 0, evals = 0, opened = 0;
     uint32_t sp = n > 1 ? 1u : 0u, ln = 0, np = 0;
     bool saturated = false;
@@ -218,63 +250,73 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
                 const uint32_t lj = lid[j];
-                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
-                if (merging && lj < N && active && lj != g) {
-                    // penetration with the leaf's body; a task when positive
-                    // and this body's index is the smaller
-                    const float pen = my_rad + b.leaf_rad[lj] - sqrtf(rx * rx + ry * ry + rz * rz);
-                    if (pen > 0.0f) {
-                        const uint32_t bi = b.idx_in[g], oi = b.idx_in[lj];
-                        if (bi < oi) {
-                            const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
-                            if (slot < N) {
-                                b.mq->pairs[slot] = make_uint2(bi, oi);
-                                b.mkeys[slot] = ((unsigned long long)g << 32) | seq;
+#pragma unroll
+                for (int q = 0; q < GW_BPL; ++q) {
+                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                    if (merging && lj < N && actq[q] && lj != gq[q]) {
+                        // penetration with the leaf's body; a task when
+                        // positive and this body's index is the smaller
+                        const float pen = my_rad[q] + b.leaf_rad[lj] - sqrtf(rx * rx + ry * ry + rz * rz);
+                        if (pen > 0.0f) {
+                            const uint32_t bi = b.idx_in[gq[q]], oi = b.idx_in[lj];
+                            if (bi < oi) {
+                                const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
+                                if (slot < N) {
+                                    b.mq->pairs[slot] = make_uint2(bi, oi);
+                                    b.mkeys[slot] = ((unsigned long long)gq[q] << 32) | seq[q];
+                                }
+                                ++seq[q];
                             }
-                            ++seq;
                         }
                     }
-                }
-                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-                const float inv = rsqrtf(rr);
-                const bool self = self_check && lj == g;
-                const float f = self ? 0.0f : c.w * (inv * inv * inv);
-                const float ph = self ? 0.0f : -c.w * inv;
-                if (PREC && lj < N) {
-                    kahan_add(nx_, cx_, f * rx);
-                    kahan_add(ny_, cy_, f * ry);
-                    kahan_add(nz_, cz_, f * rz);
-                    if (want_pot) kahan_add(np_, cp_, ph);
-                } else {
-                    ax = __fmaf_rn(f, rx, ax);
-                    ay = __fmaf_rn(f, ry, ay);
-                    az = __fmaf_rn(f, rz, az);
-                    if (want_pot) pot += ph;
+                    const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                    const float inv = rsqrtf(rr);
+                    const bool self = self_check && lj == gq[q];
+                    const float f = self ? 0.0f : c.w * (inv * inv * inv);
+                    const float ph = self ? 0.0f : -c.w * inv;
+                    if (PREC && lj < N) {
+                        kahan_add(nx_[q], cx_[q], f * rx);
+                        kahan_add(ny_[q], cy_[q], f * ry);
+                        kahan_add(nz_[q], cz_[q], f * rz);
+                        if (want_pot) kahan_add(np_[q], cp_[q], ph);
+                    } else {
+                        ax[q] = __fmaf_rn(f, rx, ax[q]);
+                        ay[q] = __fmaf_rn(f, ry, ay[q]);
+                        az[q] = __fmaf_rn(f, rz, az[q]);
+                        if (want_pot) pot[q] += ph;
+                    }
                 }
             }
         } else if (self_check) {
-#pragma unroll 4
+#pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
-                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
-                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-                const float inv = rsqrtf(rr);
-                const float f = (lid[j] == g) ? 0.0f : c.w * (inv * inv * inv);
-                ax = __fmaf_rn(f, rx, ax);
-                ay = __fmaf_rn(f, ry, ay);
-                az = __fmaf_rn(f, rz, az);
+                const uint32_t lj = lid[j];
+#pragma unroll
+                for (int q = 0; q < GW_BPL; ++q) {
+                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                    const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                    const float inv = rsqrtf(rr);
+                    const float f = (lj == gq[q]) ? 0.0f : c.w * (inv * inv * inv);
+                    ax[q] = __fmaf_rn(f, rx, ax[q]);
+                    ay[q] = __fmaf_rn(f, ry, ay[q]);
+                    az[q] = __fmaf_rn(f, rz, az[q]);
+                }
             }
         } else {
-#pragma unroll 4
+#pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
                 const float4 c = lcm[j];
-                const float rx = c.x - pw.x, ry = c.y - pw.y, rz = c.z - pw.z;
-                const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-                const float inv = rsqrtf(rr);
-                const float f = c.w * (inv * inv * inv);
-                ax = __fmaf_rn(f, rx, ax);
-                ay = __fmaf_rn(f, ry, ay);
-                az = __fmaf_rn(f, rz, az);
+#pragma unroll
+                for (int q = 0; q < GW_BPL; ++q) {
+                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                    const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                    const float inv = rsqrtf(rr);
+                    const float f = c.w * (inv * inv * inv);
+                    ax[q] = __fmaf_rn(f, rx, ax[q]);
+                    ay[q] = __fmaf_rn(f, ry, ay[q]);
+                    az[q] = __fmaf_rn(f, rz, az[q]);
+                }
             }
         }
         inter += cnt;
@@ -443,31 +485,33 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     if (ln) flush(ln);
     (void)saturated;
 
-    // counters: interactions count the active lanes of every list entry
-    const uint32_t act = __popc(__ballot_sync(0xffffffffu, active));
+    // counters: interactions count the group's bodies for every list entry
     if (lane == 0) {
-        atomicAdd(&b.st->interactions, (unsigned long long)inter * act);
+        atomicAdd(&b.st->interactions, (unsigned long long)inter * grp.y);
         atomicAdd(&b.st->mac_evals, (unsigned long long)evals);
         atomicAdd(&b.st->opened, (unsigned long long)opened);
     }
-    if (active) {
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) {
+        if (!actq[q]) continue;
         // body index and position again (not kept live through the walk)
-        const uint32_t bi = b.idx_in[g];
-        const float4 pm = b.leaf_pm[g];
+        const uint32_t bi = b.idx_in[gq[q]];
+        const float4 pm = b.leaf_pm[gq[q]];
+        float fx = ax[q], fy = ay[q], fz = az[q], fp = pot[q];
         if (PREC) {
-            ax = ax + (nx_ - cx_);
-            ay = ay + (ny_ - cy_);
-            az = az + (nz_ - cz_);
-            pot = pot + (np_ - cp_);
+            fx = fx + (nx_[q] - cx_[q]);
+            fy = fy + (ny_[q] - cy_[q]);
+            fz = fz + (nz_[q] - cz_[q]);
+            fp = fp + (np_[q] - cp_[q]);
         }
-        if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(ax, ay, az, 0.0f);
-        if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
-        if (want_pot) b.potential[bi] = pot;
+        if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(fx, fy, fz, 0.0f);
+        if (b.accel_mag) b.accel_mag[bi] = sqrtf(fx * fx + fy * fy + fz * fz);
+        if (want_pot) b.potential[bi] = fp;
         const float4 vd = ld_vel_density(b.bodies_in, bi);
         if (PREC)
-            walk_update_fp64(b, P, sim, bi, pm, vd, ax, ay, az);
+            walk_update_fp64(b, P, sim, bi, pm, vd, fx, fy, fz);
         else
-            walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
+            walk_update(b, P, sim, bi, pm, vd, fx, fy, fz);
     }
     __syncwarp();
     }  // groups

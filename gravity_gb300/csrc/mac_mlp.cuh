@@ -1,5 +1,5 @@
 // mac_mlp.cuh — the learned multipole-acceptance criterion: features of a
-// (32-body group, node) pair and the 12-32-32-1 MLP evaluated per warp on the
+// (body group, node) pair and the 12-32-32-1 MLP evaluated per warp on the
 // tensor cores (mma.sync m16n8k16, BF16 operands, FP32 accumulation).
 //
 // The MLP predicts log10 of the relative error of replacing the node by its
@@ -340,8 +340,14 @@ __device__ __forceinline__ void mac_load_frag(MacDeviceWeights& mw, uint32_t* sm
 }
 
 // smallest |a| of the group's bodies in the previous step (feature 8)
-__device__ __forceinline__ float group_accel_ref(const StepBuffers& b, bool active, uint32_t bi) {
-    float a = (active && b.accel_mag) ? b.accel_mag[bi] : 3.0e38f;
+// (act[q], slot[q]: the lane's bodies, q < BPL)
+template <int BPL>
+__device__ __forceinline__ float group_accel_ref(const StepBuffers& b, const bool (&act)[BPL],
+                                                 const uint32_t (&slot)[BPL]) {
+    float a = 3.0e38f;
+#pragma unroll
+    for (int q = 0; q < BPL; ++q)
+        if (act[q] && b.accel_mag) a = fminf(a, b.accel_mag[b.idx_in[slot[q]]]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) a = fminf(a, __shfl_xor_sync(0xffffffffu, a, o));
     return a < 3.0e38f ? a : 0.0f;

@@ -66,7 +66,7 @@ extern "C" {
 #define GBH_BOUNDS_DYNAMIC 1u
 /* acceptance criterion of the walk (new in this library) */
 #define GBH_MAC_PLAIN 0u    /* reference rule: (longest AABB side / 2) * invDist < theta, per body */
-#define GBH_MAC_LEARNED 1u  /* learned MLP criterion, one decision per (32-body group, node) */
+#define GBH_MAC_LEARNED 1u  /* learned MLP criterion, one decision per (body group of up to 64, node) */
 #define GBH_MAC_GROUP 2u    /* group theta rule used as the learned criterion's ablation */
 /* precision form (new in this library) */
 #define GBH_PRECISION_FP32 0u     /* reference arithmetic */
@@ -331,7 +331,7 @@ int gbh_mac_get_weights(gbh_ctx* ctx, float* params, uint32_t count);
  * 0.25 and 1.0.  Training pairs are recorded in the same band. */
 int gbh_mac_set_band(gbh_ctx* ctx, float theta_accept, float theta_open);
 int gbh_mac_get_band(gbh_ctx* ctx, float* theta_accept, float* theta_open);
-/* Sample (32-body group, node) pairs from the current tree, compute their
+/* Sample (body group, node) pairs from the current tree, compute their
  * features and labels (log10 of the relative error of accepting the node's
  * monopole against its exact subtree sum, max over the group) into device
  * buffers owned by the context.  Returns the number of pairs written. */
