@@ -99,6 +99,13 @@ struct StepBuffers {
     float4* accel;
     float* accel_mag;     // |acceleration| of the last walk, by body id (learned MAC feature)
     uint32_t* node_lo;    // first sorted slot of each internal node's leaf range
+    // compact topology written by the build and read by the fill, which then
+    // writes whole 80-byte nodes (no partial-sector writes to the node arrays)
+    uint2* topo_kids;      // (childA, childB) per internal node
+    uint32_t* topo_cnt;    // bodiesContained per internal node
+    uint32_t* fill_ready;  // arrival counters of the fill's climb across tiles
+    uint32_t* parent_int;  // parentId per internal node
+    uint32_t* parent_leaf; // parentId per leaf
     uint2* groups;        // (first slot, body count) of the group walk's body groups
     uint2* fill_frontier; // (node, bodies) handed from the tiled fill to the top-tree fill
     uint32_t fill_frontier_cap;
@@ -287,6 +294,7 @@ void launch_prepare(const StepBuffers& b, cudaStream_t s);
 void launch_sort(const StepBuffers& b, cudaStream_t s);
 void launch_build(const StepBuffers& b, cudaStream_t s);
 void launch_fill(const StepBuffers& b, cudaStream_t s);
+void launch_build_nodes(const StepBuffers& b, cudaStream_t s);
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s);
 void launch_init_pos64(const gbh_body* bodies, double* pos64, uint32_t N, cudaStream_t s);
 void launch_round_pos64(gbh_body* bodies, const double* pos64, uint32_t offset, uint32_t count, cudaStream_t s);

@@ -74,6 +74,11 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.accel = c->accel;
     b.accel_mag = c->accel_mag;
     b.node_lo = c->node_lo;
+    b.topo_kids = c->topo_kids;
+    b.topo_cnt = c->topo_cnt;
+    b.fill_ready = c->fill_ready;
+    b.parent_int = c->parent_int;
+    b.parent_leaf = c->parent_leaf;
     b.groups = c->groups;
     // the fill's frontier lives in the sort's spare key buffer (free once the
     // sorted keys are back in keys_in, until the next step's encode)
@@ -266,6 +271,8 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_locks = A.add((size_t)n * 4), o_conf = A.add((size_t)n * 4);
     size_t o_accel = A.add((size_t)n * 16), o_amag = A.add((size_t)n * 4);
     size_t o_nlo = A.add((size_t)ni * 4), o_groups = A.add((size_t)n * 8);
+    size_t o_tkids = A.add((size_t)ni * 8), o_tcnt = A.add((size_t)ni * 4), o_tready = A.add((size_t)ni * 4);
+    size_t o_pint = A.add((size_t)ni * 4), o_pleaf = A.add((size_t)n * 4);
     size_t o_tdead = A.add((size_t)c->prep_tiles_cap * 4), o_taabb = A.add((size_t)c->prep_tiles_cap * 24);
     size_t o_hist = A.add(SORT_PASSES * SORT_RADIX * 4), o_bbase = A.add(SORT_PASSES * SORT_RADIX * 4);
     c->lookback_bytes = (size_t)SORT_PASSES * c->sort_tiles_cap * SORT_RADIX * 4;
@@ -298,6 +305,11 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->conflicts = (uint32_t*)(base + o_conf);
     c->accel = (float4*)(base + o_accel);
     c->accel_mag = (float*)(base + o_amag);
+    c->topo_kids = (uint2*)(base + o_tkids);
+    c->topo_cnt = (uint32_t*)(base + o_tcnt);
+    c->fill_ready = (uint32_t*)(base + o_tready);
+    c->parent_int = (uint32_t*)(base + o_pint);
+    c->parent_leaf = (uint32_t*)(base + o_pleaf);
     c->node_lo = (uint32_t*)(base + o_nlo);
     c->groups = (uint2*)(base + o_groups);
     c->tile_dead = (uint32_t*)(base + o_tdead);
@@ -661,7 +673,17 @@ int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) {
 }
 int gbh_stage_prepare(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_prepare); }
 int gbh_stage_sort(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_sort); }
-int gbh_stage_build(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_build); }
+int gbh_stage_build(gbh_ctx* c) {
+    int rc = stage_common(c, nullptr);
+    if (rc) return rc;
+    if ((rc = enqueue_build(c))) return rc;
+    // the stage boundary of the reference: its Node topology words as
+    // buildBinaryRadixTree leaves them (the step itself goes straight to the
+    // fill, which writes whole nodes)
+    launch_build_nodes(ctx_buffers(c), c->stream);
+    if ((rc = check_launch(c, "build nodes"))) return rc;
+    return gbh_synchronize(c);
+}
 int gbh_stage_fill(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_fill); }
 int gbh_stage_walk(gbh_ctx* c, const gbh_step_params* p) {
     int rc = stage_common(c, p);

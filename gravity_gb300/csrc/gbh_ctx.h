@@ -41,6 +41,11 @@ struct gbh_ctx {
     float4* accel = nullptr;
     float* accel_mag = nullptr;
     uint32_t* node_lo = nullptr;
+    uint2* topo_kids = nullptr;
+    uint32_t* topo_cnt = nullptr;
+    uint32_t* fill_ready = nullptr;
+    uint32_t* parent_int = nullptr;
+    uint32_t* parent_leaf = nullptr;
     uint2* groups = nullptr;
     uint32_t* tile_dead = nullptr;
     float* tile_aabb = nullptr;

@@ -1,10 +1,12 @@
 // k_tree.cu — Karras LBVH build and single-pass bottom-up fill.
 //
 // Build: treeBuildBinaryRadixTreeKernel (SH/compute/tree/bh_tree.comp:43-133),
-//   one thread per internal node, integer-exact.  Like the reference it writes
-//   the topology words (childA/B, parentId, bodiesContained, nodeDepth =
-//   min(i, j), readyChildren = 0); the COM/AABB/colour words it also zeroes are
-//   rewritten by the fill before anything reads them, so they are not written.
+//   one thread per internal node, integer-exact.  It writes the topology into
+//   compact arrays (children, counts, first slots, parents, arrival counters)
+//   instead of the 80-byte nodes; the fill then writes every node whole, all
+//   its words including the topology ones, so no sector of the node arrays is
+//   written in part.  The stage entry point gbh_stage_build also writes the
+//   reference's intermediate topology words into the nodes (k_build_nodes).
 // Fill: treeInitLeafNodesKernel (bh_tree.comp:140-175) + 64 launches of
 //   treePropagateNodesKernel (bh_tree.comp:183-259) become one kernel: each
 //   leaf thread initialises its leaf and climbs; at every internal node an
@@ -32,15 +34,14 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     const uint64_t* keys = b.keys_in;
     if (n <= 1) {
         if (n == 1 && gid == 0) {
-            // single body, bh_tree.comp:46-62
-            gbh_node* r = &b.internal[0];
-            r->child_a = 0;
-            r->child_b = GBH_NONE;
-            r->ready_children = 1;
-            r->node_depth = 0;
-            r->bodies_contained = 0;
-            r->parent_id = GBH_NONE;
-            b.leaf[0].parent_id = N;
+            // single body, bh_tree.comp:46-62: root with one child, bodiesContained 0,
+            // readyChildren 1
+            b.topo_kids[0] = make_uint2(0u, GBH_NONE);
+            b.topo_cnt[0] = 0;
+            b.node_lo[0] = 0;
+            b.fill_ready[0] = 1;
+            b.parent_int[0] = GBH_NONE;
+            b.parent_leaf[0] = N;
         }
         return;
     }
@@ -67,18 +68,39 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     const int mn = min(i, j), mx = max(i, j);
     const uint32_t left = (mn == gamma) ? (uint32_t)gamma : (uint32_t)gamma + N;
     const uint32_t right = (mx == gamma + 1) ? (uint32_t)(gamma + 1) : (uint32_t)(gamma + 1) + N;
-    gbh_node* nd = &b.internal[i];
-    // words @40..@59: childA, childB, nodeDepth, bodiesContained, readyChildren
-    nd->child_a = left;
-    nd->child_b = right;
-    nd->node_depth = (uint32_t)mn;
+    b.topo_kids[i] = make_uint2(left, right);
     b.node_lo[i] = (uint32_t)mn;
-    nd->bodies_contained = (uint32_t)(mx - mn + 1);
-    nd->ready_children = 0;
+    b.topo_cnt[i] = (uint32_t)(mx - mn + 1);
+    b.fill_ready[i] = 0;
     const uint32_t self = (uint32_t)i + N;
-    if (left < N) b.leaf[left].parent_id = self; else b.internal[left - N].parent_id = self;
-    if (right < N) b.leaf[right].parent_id = self; else b.internal[right - N].parent_id = self;
-    if (i == 0) nd->parent_id = GBH_NONE;
+    if (left < N) b.parent_leaf[left] = self; else b.parent_int[left - N] = self;
+    if (right < N) b.parent_leaf[right] = self; else b.parent_int[right - N] = self;
+    if (i == 0) b.parent_int[0] = GBH_NONE;
+}
+
+// The reference's Node topology words after buildBinaryRadixTree (childA/B,
+// nodeDepth = min(i, j), bodiesContained, readyChildren = 0, parentId; leaves:
+// parentId), for the stage-level API.
+__global__ void k_build_nodes(StepBuffers b) {
+    const uint32_t n = b.st->n_new;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n == 0) return;
+    const uint32_t ni = n > 1 ? n - 1 : 1;
+    if (t < ni) {
+        gbh_node* nd = &b.internal[t];
+        const uint2 k = b.topo_kids[t];
+        nd->child_a = k.x;
+        nd->child_b = k.y;
+        nd->node_depth = b.node_lo[t];
+        nd->bodies_contained = b.topo_cnt[t];
+        nd->ready_children = b.fill_ready[t];
+        nd->parent_id = b.parent_int[t];
+    }
+    if (t < n) b.leaf[t].parent_id = b.parent_leaf[t];
+}
+
+void launch_build_nodes(const StepBuffers& b, cudaStream_t s) {
+    k_build_nodes<<<(b.N + 255) / 256, 256, 0, s>>>(b);
 }
 
 void launch_build(const StepBuffers& b, cudaStream_t s) {
@@ -186,19 +208,17 @@ __device__ __forceinline__ NodeVals combine(const NodeVals& L, const NodeVals& R
     return out;
 }
 
-// Write a finished internal node: its Node words (reference layout), the
-// walk records of its two children, and mark it claimed (readyChildren =
-// 0xFFFFFFFF, bh_tree.comp:200).
+// Write a finished internal node whole: its Node words (reference layout,
+// common.glsl:40-58) including the topology ones, readyChildren claimed
+// (0xFFFFFFFF, bh_tree.comp:200), and the walk records of its two children.
 __device__ __forceinline__ void store_internal(const StepBuffers& b, uint32_t i, const NodeVals& out, const NodeVals& L,
                                                const NodeVals& R, uint32_t a_id, uint32_t b_id, uint32_t a_count,
-                                               uint32_t b_count) {
-    gbh_node* nd = &b.internal[i];
-    float4* np = reinterpret_cast<float4*>(nd);
+                                               uint32_t b_count, uint32_t bodies, uint32_t parent) {
+    float4* np = reinterpret_cast<float4*>(&b.internal[i]);
     __stcg(np + 0, out.cm);
     __stcg(np + 1, make_float4(out.box[0], out.box[1], out.box[2], out.box[3]));
-    __stcg(reinterpret_cast<float2*>(np + 2), make_float2(out.box[4], out.box[5]));
-    nd->node_depth = out.depth;
-    nd->ready_children = GBH_NONE;
+    __stcg(reinterpret_cast<uint4*>(np + 2), make_uint4(__float_as_uint(out.box[4]), __float_as_uint(out.box[5]), a_id, b_id));
+    __stcg(reinterpret_cast<uint4*>(np + 3), make_uint4(out.depth, bodies, GBH_NONE, parent));
     __stcg(np + 4, out.col);
     ChildPair pr;
     pr.a = make_rec(L, a_id, a_count, a_id < b.N);
@@ -265,7 +285,7 @@ __global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
     TileVals* s_node = s_leaf + FILL_TILE;                       // [FILL_TILE]
     uint4* s_topo = reinterpret_cast<uint4*>(s_node + FILL_TILE);  // childA, childB, first slot, bodies
     uint32_t* s_parent = reinterpret_cast<uint32_t*>(s_topo + FILL_TILE);
-    uint32_t* s_ready = s_parent + FILL_TILE;
+    uint32_t* s_ready = s_parent + FILL_TILE;  // arrival counters of the tile's internal nodes
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
     const uint32_t base = blockIdx.x * FILL_TILE;
@@ -276,10 +296,9 @@ __global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
     s_ready[t] = 0u;
     if (g + 1 < n) {
         // topology of internal node g (written by the build), read once
-        const gbh_node* nd = &b.internal[g];
-        const uint2 kids = __ldg(reinterpret_cast<const uint2*>(&nd->child_a));
-        s_topo[t] = make_uint4(kids.x, kids.y, __ldg(&b.node_lo[g]), __ldg(&nd->bodies_contained));
-        s_parent[t] = __ldg(&nd->parent_id);
+        const uint2 kids = b.topo_kids[g];
+        s_topo[t] = make_uint4(kids.x, kids.y, b.node_lo[g], b.topo_cnt[g]);
+        s_parent[t] = b.parent_int[g];
     }
     NodeVals own;
     uint32_t parent0 = GBH_NONE;
@@ -290,7 +309,7 @@ __global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
         // leaf init, bh_tree.comp:153-166
         gbh_node* lf = &b.leaf[g];
         float4* lp = reinterpret_cast<float4*>(lf);
-        parent0 = lf->parent_id;
+        parent0 = b.parent_leaf[g];
         own.cm = pm;
         own.box[0] = own.box[3] = pm.x;
         own.box[1] = own.box[4] = pm.y;
@@ -350,7 +369,7 @@ __global__ __launch_bounds__(FILL_TILE) void k_fill(StepBuffers b) {
         const NodeVals out = combine(L, R);
         const uint32_t a_id = self_is_a ? self : sib, b_id = self_is_a ? sib : self;
         store_internal(b, i, out, L, R, a_id, b_id, self_is_a ? self_count : sib_count,
-                       self_is_a ? sib_count : self_count);
+                       self_is_a ? sib_count : self_count, topo.w, s_parent[i - base]);
         s_node[i - base] = to_tile(out);
         self = node;
         self_count += sib_count;
@@ -380,11 +399,10 @@ __device__ void climb_global(const StepBuffers& b, uint32_t self, uint32_t self_
     const uint32_t N = b.N;
     while (node != GBH_NONE) {
         const uint32_t i = node - N;
-        gbh_node* nd = &b.internal[i];
         // release: own node's writes before the count; acquire: the sibling's writes after it
-        const uint32_t old = atomic_add_acq_rel(&nd->ready_children, 1u);
+        const uint32_t old = atomic_add_acq_rel(&b.fill_ready[i], 1u);
         if (old == 0u) return;
-        const uint2 kids = *reinterpret_cast<const uint2*>(&nd->child_a);
+        const uint2 kids = b.topo_kids[i];
         const bool self_is_a = kids.x == self;
         const uint32_t sib = self_is_a ? kids.y : kids.x;
         NodeVals S;
@@ -400,18 +418,18 @@ __device__ void climb_global(const StepBuffers& b, uint32_t self, uint32_t self_
             S = load_node_cg(&b.leaf[sib]);
         } else {
             S = load_node_cg(&b.internal[sib - N]);
-            sib_count = __ldcg(&b.internal[sib - N].bodies_contained);
+            sib_count = b.topo_cnt[sib - N];
         }
         const NodeVals& L = self_is_a ? own : S;
         const NodeVals& R = self_is_a ? S : own;
         const NodeVals out = combine(L, R);
         const uint32_t a_id = self_is_a ? self : sib, b_id = self_is_a ? sib : self;
+        const uint32_t parent = b.parent_int[i];
         store_internal(b, i, out, L, R, a_id, b_id, self_is_a ? self_count : sib_count,
-                       self_is_a ? sib_count : self_count);
+                       self_is_a ? sib_count : self_count, b.topo_cnt[i], parent);
         self = node;
         self_count = self_count + sib_count;
         own = out;
-        const uint32_t parent = nd->parent_id;
         if (parent == GBH_NONE) {
             b.st->tree_height = out.depth;
             *b.root_rec = make_rec(out, node, self_count, false);
@@ -429,7 +447,7 @@ __global__ __launch_bounds__(256) void k_fill_top(StepBuffers b) {
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
         const uint2 fr = b.fill_frontier[e];
         const gbh_node* nd = fr.x < N ? &b.leaf[fr.x] : &b.internal[fr.x - N];
-        climb_global(b, fr.x, fr.y, load_node_cg(nd), __ldcg(&nd->parent_id));
+        climb_global(b, fr.x, fr.y, load_node_cg(nd), fr.x < N ? b.parent_leaf[fr.x] : b.parent_int[fr.x - N]);
     }
 }
 

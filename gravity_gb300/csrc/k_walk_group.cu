@@ -84,11 +84,8 @@ __global__ void k_find_groups(StepBuffers b) {
     uint2 mine[2];
     uint32_t k = 0;
     if (t + 1 < n) {
-        // childA, childB (Node words @40, @44) and bodiesContained (@52); the
-        // node is 80 bytes, so these are 8-byte aligned pairs
-        const uint2 kids = __ldg(reinterpret_cast<const uint2*>(&b.internal[t].child_a));
-        const uint32_t cnt = __ldg(&b.internal[t].bodies_contained);
-        const uint2 w = kids;
+        const uint2 w = b.topo_kids[t];
+        const uint32_t cnt = b.topo_cnt[t];
         if (cnt > GBH_GROUP_MAX) {
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
@@ -96,8 +93,8 @@ __global__ void k_find_groups(StepBuffers b) {
                 if (ch < N) {
                     mine[k++] = make_uint2(ch, 1u);
                 } else {
-                    const uint32_t cc = __ldg(&b.internal[ch - N].bodies_contained);
-                    if (cc <= GBH_GROUP_MAX) mine[k++] = make_uint2(__ldg(&b.node_lo[ch - N]), cc);
+                    const uint32_t cc = b.topo_cnt[ch - N];
+                    if (cc <= GBH_GROUP_MAX) mine[k++] = make_uint2(b.node_lo[ch - N], cc);
                 }
             }
         } else if (t == 0) {
