@@ -210,7 +210,8 @@ __device__ __forceinline__ NodeVals combine(const NodeVals& L, const NodeVals& R
 
 // Write a finished internal node whole: its Node words (reference layout,
 // common.glsl:40-58) including the topology ones, readyChildren claimed
-// (0xFFFFFFFF, bh_tree.comp:200), and the walk records of its two children.
+// (0xFFFFFFFF, bh_tree.comp:200), and, for the plain walk, the walk records
+// of its two children.
 __device__ __forceinline__ void store_internal(const StepBuffers& b, uint32_t i, const NodeVals& out, const NodeVals& L,
                                                const NodeVals& R, uint32_t a_id, uint32_t b_id, uint32_t a_count,
                                                uint32_t b_count, uint32_t bodies, uint32_t parent) {
@@ -220,10 +221,13 @@ __device__ __forceinline__ void store_internal(const StepBuffers& b, uint32_t i,
     __stcg(reinterpret_cast<uint4*>(np + 2), make_uint4(__float_as_uint(out.box[4]), __float_as_uint(out.box[5]), a_id, b_id));
     __stcg(reinterpret_cast<uint4*>(np + 3), make_uint4(out.depth, bodies, GBH_NONE, parent));
     __stcg(np + 4, out.col);
-    ChildPair pr;
-    pr.a = make_rec(L, a_id, a_count, a_id < b.N);
-    pr.b = make_rec(R, b_id, b_count, b_id < b.N);
-    b.pairs[i] = pr;
+    // the children's walk records feed the plain walk only
+    if (b.params->mac_mode == GBH_MAC_PLAIN) {
+        ChildPair pr;
+        pr.a = make_rec(L, a_id, a_count, a_id < b.N);
+        pr.b = make_rec(R, b_id, b_count, b_id < b.N);
+        b.pairs[i] = pr;
+    }
 }
 
 // Node values kept in shared memory by the tiled fill (64 bytes)
