@@ -312,7 +312,7 @@ PLAIN_THETAS = [0.3, 0.5, 0.7]
 # dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture
 # (profiles/walk_learned_mixture4M.md), divided by its bodies; the walk's
 # traffic grows in proportion to the bodies
-WALK_LEARNED_DRAM_BYTES_PER_BODY = None
+WALK_LEARNED_DRAM_BYTES_PER_BODY = 298.6
 
 
 def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
@@ -381,6 +381,8 @@ def run_ours(args):
     units = abi.units(G=1.0)
     p_plain = wl["params"]
     merging = p_plain.merging_collision_or_neither != abi.MODE_NEITHER
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(local)[0]  # before the context: its footprint is the difference
     bh = BarnesHut(wl["n"], bounds, units, device=local)
     bh.upload_bodies(bodies)
     bh.init()
@@ -406,7 +408,6 @@ def run_ours(args):
     p_head = p_plain
     mac_name = "plain"
     precision = bool(wl.get("precision"))
-    free0 = torch.cuda.mem_get_info(local)[0]
     if precision:
         p_head, calib = precision_arm(bh, p_plain, accuracy)
         mac_name = "plain+compensated"
