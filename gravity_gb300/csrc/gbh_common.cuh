@@ -62,6 +62,7 @@ struct DevState {
     uint32_t num_groups;               // body groups of the group walk
     uint32_t frontier_saturated;       // group walks that accepted instead of opening (full stack)
     uint32_t fill_frontier;            // nodes handed from the tiled fill to the top-tree fill
+    uint32_t sorted_valid;             // sorted_pm holds the current positions in index order
     unsigned long long interactions;
     unsigned long long opened;
     unsigned long long mac_evals;
@@ -88,6 +89,8 @@ struct StepBuffers {
     ChildPair* pairs;     // per internal node
     WalkRec* root_rec;    // record of the root (internal node 0)
     float4* leaf_pm;      // sorted-order copy of posMass (leaf comMass)
+    float4* sorted_pm;    // posMass after the walk's update, by the walk's sorted slot: the next
+                          // step's compaction and encode read it in order instead of gathering
     float* leaf_rad;      // sorted-order radius(body)
     gbh_sim_values* sim;
     DevState* st;
@@ -220,7 +223,8 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // Symplectic update and static bounds of one body after its walk
 // (bh_force.comp:117-141); writes the output body buffer.
 __device__ __forceinline__ void walk_update(const StepBuffers& b, const gbh_step_params* P, const gbh_sim_values* sim,
-                                            uint32_t bi, float4 pm, float4 vd, float ax, float ay, float az) {
+                                            uint32_t g, uint32_t bi, float4 pm, float4 vd, float ax, float ay,
+                                            float az) {
     const float dt = P->dt;
     const float nvx = vd.x + ax * dt, nvy = vd.y + ay * dt, nvz = vd.z + az * dt;
     float npx = pm.x + nvx * dt, npy = pm.y + nvy * dt, npz = pm.z + nvz * dt;
@@ -235,12 +239,14 @@ __device__ __forceinline__ void walk_update(const StepBuffers& b, const gbh_step
         } else if (pm.x < mn[0] || pm.x > mx[0] || pm.y < mn[1] || pm.y > mx[1] || pm.z < mn[2] || pm.z > mx[2]) {
             const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
             st_body(b.bodies_out, bi, z, z);
+            b.sorted_pm[g] = z;
             atomicAdd(&b.sim->out_of_bounds, 1u);
             atomicAdd(&b.st->oob, 1u);
             return;
         }
     }
     st_body(b.bodies_out, bi, make_float4(npx, npy, npz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
+    b.sorted_pm[g] = make_float4(npx, npy, npz, pm.w);
 }
 
 // The update of the precision form: the kick in FP32 as above, the drift in
@@ -248,8 +254,8 @@ __device__ __forceinline__ void walk_update(const StepBuffers& b, const gbh_step
 // the FP32 rounding of the new position.  Static bounds as walk_update, the
 // wrap in FP64.
 __device__ __forceinline__ void walk_update_fp64(const StepBuffers& b, const gbh_step_params* P,
-                                                 const gbh_sim_values* sim, uint32_t bi, float4 pm, float4 vd,
-                                                 float ax, float ay, float az) {
+                                                 const gbh_sim_values* sim, uint32_t g, uint32_t bi, float4 pm,
+                                                 float4 vd, float ax, float ay, float az) {
     const float dt = P->dt;
     const float nvx = vd.x + ax * dt, nvy = vd.y + ay * dt, nvz = vd.z + az * dt;
     const double2 xy = reinterpret_cast<const double2*>(b.pos64_in)[2 * (size_t)bi];
@@ -270,6 +276,7 @@ __device__ __forceinline__ void walk_update_fp64(const StepBuffers& b, const gbh
             st_body(b.bodies_out, bi, z, z);
             reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi] = make_double2(0.0, 0.0);
             reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi + 1] = make_double2(0.0, 0.0);
+            b.sorted_pm[g] = z;
             atomicAdd(&b.sim->out_of_bounds, 1u);
             atomicAdd(&b.st->oob, 1u);
             return;
@@ -278,6 +285,7 @@ __device__ __forceinline__ void walk_update_fp64(const StepBuffers& b, const gbh
     reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi] = make_double2(px, py);
     reinterpret_cast<double2*>(b.pos64_out)[2 * (size_t)bi + 1] = make_double2(pz, 0.0);
     st_body(b.bodies_out, bi, make_float4((float)px, (float)py, (float)pz, pm.w), make_float4(nvx, nvy, nvz, vd.w));
+    b.sorted_pm[g] = make_float4((float)px, (float)py, (float)pz, pm.w);
 }
 
 // Kahan-compensated accumulation (sum, c): sum + (x - c), c the lost low part

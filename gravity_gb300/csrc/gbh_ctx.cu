@@ -64,6 +64,7 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.root_rec = c->root_rec;
     b.leaf_pm = c->leaf_pm;
     b.leaf_rad = c->leaf_rad;
+    b.sorted_pm = c->sorted_pm;
     b.sim = c->sim;
     b.st = c->st;
     b.params = c->params_dev;
@@ -187,6 +188,14 @@ static int ensure_precision_buffers(gbh_ctx* c) {
     return GBH_OK;
 }
 
+// The next compaction gathers the positions through the index instead of
+// reading the last walk's in-order copy (after any eager stage call, upload or
+// write that the step graph does not see).
+static int invalidate_sorted(gbh_ctx* c) {
+    CUDA_TRY(c, cudaMemsetAsync(&c->st->sorted_valid, 0, 4, c->stream));
+    return GBH_OK;
+}
+
 // Before a precision-form step: FP64 positions from the body buffer when they
 // are not current (first such step, after an upload or an FP32 step).
 static int prepare_precision(gbh_ctx* c) {
@@ -264,7 +273,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_idx0 = A.add((size_t)n * 4), o_idx1 = A.add((size_t)n * 4);
     size_t o_leaf = A.add((size_t)n * 80), o_int = A.add((size_t)ni * 80);
     size_t o_pairs = A.add((size_t)ni * sizeof(ChildPair)), o_root = A.add(sizeof(WalkRec));
-    size_t o_lpm = A.add((size_t)n * 16), o_lrad = A.add((size_t)n * 4);
+    size_t o_lpm = A.add((size_t)n * 16), o_lrad = A.add((size_t)n * 4), o_spm = A.add((size_t)n * 16);
     size_t o_sim = A.add(sizeof(gbh_sim_values)), o_st = A.add(sizeof(DevState));
     size_t o_par = A.add(sizeof(gbh_step_params));
     size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8);
@@ -296,6 +305,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->root_rec = (WalkRec*)(base + o_root);
     c->leaf_pm = (float4*)(base + o_lpm);
     c->leaf_rad = (float*)(base + o_lrad);
+    c->sorted_pm = (float4*)(base + o_spm);
     c->sim = (gbh_sim_values*)(base + o_sim);
     c->st = (DevState*)(base + o_st);
     c->params_dev = (gbh_step_params*)(base + o_par);
@@ -371,9 +381,11 @@ int gbh_upload_bodies(gbh_ctx* c, const gbh_body* host, uint32_t count, uint32_t
     CUDA_TRY(c, cudaSetDevice(c->device));
     CUDA_TRY(c, cudaMemcpyAsync(c->bodies[c->bin] + offset, host, (size_t)count * sizeof(gbh_body),
                                 cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->pos64_valid = false;
     ++c->state_epoch;
+    int rc = invalidate_sorted(c);
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return GBH_OK;
 }
 
@@ -383,6 +395,7 @@ int gbh_init(gbh_ctx* c) {
     launch_init_index(c->idx[c->iin], c->N, c->sim, &c->units, c->stream);
     int rc = check_launch(c, "init");
     if (rc) return rc;
+    if ((rc = invalidate_sorted(c))) return rc;
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->inited = true;
     return GBH_OK;
@@ -557,7 +570,7 @@ int gbh_write_positions_fp64(gbh_ctx* c, const double* host, uint32_t count, uin
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->pos64_valid = true;
     ++c->state_epoch;
-    return GBH_OK;
+    return invalidate_sorted(c);
 }
 
 int gbh_read_diagnostics(gbh_ctx* c, gbh_diagnostics* out) {
@@ -631,17 +644,23 @@ void* gbh_stream(gbh_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int gbh_write_sim_values(gbh_ctx* c, const gbh_sim_values* host) {
     if (!c || !host) return GBH_ERR_INVALID;
-    return write_dev(c, c->sim, host, sizeof(gbh_sim_values));
+    int rc = write_dev(c, c->sim, host, sizeof(gbh_sim_values));
+    if (rc) return rc;
+    return invalidate_sorted(c);
 }
 
 int gbh_write_index(gbh_ctx* c, const uint32_t* host, uint32_t count, uint32_t offset) {
     RANGE_CHECK(c, host, count, offset, c->N);
-    return write_dev(c, c->idx[c->iin] + offset, host, (size_t)count * 4);
+    int rc = write_dev(c, c->idx[c->iin] + offset, host, (size_t)count * 4);
+    if (rc) return rc;
+    return invalidate_sorted(c);
 }
 
 int gbh_write_morton(gbh_ctx* c, const uint64_t* host, uint32_t count, uint32_t offset) {
     RANGE_CHECK(c, host, count, offset, c->N);
-    return write_dev(c, c->keys[c->iin] + offset, host, (size_t)count * 8);
+    int rc = write_dev(c, c->keys[c->iin] + offset, host, (size_t)count * 8);
+    if (rc) return rc;
+    return invalidate_sorted(c);
 }
 
 // ---- stage entry points -------------------------------------------------------
@@ -655,13 +674,15 @@ static int stage_common(gbh_ctx* c, const gbh_step_params* p) {
     return GBH_OK;
 }
 
-#define STAGE_BODY(c, p, fn)          \
-    do {                              \
-        int rc_ = stage_common(c, p); \
-        if (rc_) return rc_;          \
-        rc_ = fn(c);                  \
-        if (rc_) return rc_;          \
-        return gbh_synchronize(c);    \
+// eager stages run outside the step graph: the next compaction gathers
+#define STAGE_BODY(c, p, fn)                   \
+    do {                                       \
+        int rc_ = stage_common(c, p);          \
+        if (rc_) return rc_;                   \
+        rc_ = fn(c);                           \
+        if (rc_) return rc_;                   \
+        if ((rc_ = invalidate_sorted(c))) return rc_; \
+        return gbh_synchronize(c);             \
     } while (0)
 
 int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) {
@@ -669,6 +690,7 @@ int gbh_stage_reset(gbh_ctx* c, const gbh_step_params* p) {
     if (rc) return rc;
     if ((rc = prepare_precision(c))) return rc;
     if ((rc = enqueue_reset(c))) return rc;
+    if ((rc = invalidate_sorted(c))) return rc;
     return gbh_synchronize(c);
 }
 int gbh_stage_prepare(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_prepare); }
@@ -682,6 +704,7 @@ int gbh_stage_build(gbh_ctx* c) {
     // fill, which writes whole nodes)
     launch_build_nodes(ctx_buffers(c), c->stream);
     if ((rc = check_launch(c, "build nodes"))) return rc;
+    if ((rc = invalidate_sorted(c))) return rc;
     return gbh_synchronize(c);
 }
 int gbh_stage_fill(gbh_ctx* c) { STAGE_BODY(c, nullptr, enqueue_fill); }
@@ -692,6 +715,7 @@ int gbh_stage_walk(gbh_ctx* c, const gbh_step_params* p) {
         return fail(c, GBH_ERR_STATE, "precision-form walk without current FP64 positions (run gbh_stage_reset first)");
     if ((rc = enqueue_walk(c))) return rc;
     if (c->params_host.flags & GBH_FLAG_STORE_POTENTIAL) c->potential_epoch = c->state_epoch;
+    if ((rc = invalidate_sorted(c))) return rc;
     return gbh_synchronize(c);
 }
 int gbh_stage_merge(gbh_ctx* c, const gbh_step_params* p) { STAGE_BODY(c, p, enqueue_merge); }
@@ -699,7 +723,8 @@ int gbh_stage_swap(gbh_ctx* c) {
     if (!c) return GBH_ERR_INVALID;
     int rc = enqueue_swap(c);
     after_swap(c, c->params_valid && c->params_host.precision_mode == GBH_PRECISION_COMPENSATED);
-    return rc;
+    if (rc) return rc;
+    return invalidate_sorted(c);
 }
 
 int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM_STAGES]) {
@@ -721,6 +746,7 @@ int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM
     }
     for (int i = 0; i <= GBH_NUM_STAGES; ++i) cudaEventDestroy(ev[i]);
     if (rc) return rc;
+    if ((rc = invalidate_sorted(c))) return rc;
     after_swap(c, c->params_host.precision_mode == GBH_PRECISION_COMPENSATED);
     return gbh_synchronize(c);
 }

@@ -30,6 +30,7 @@ struct gbh_ctx {
     ChildPair* pairs = nullptr;
     WalkRec* root_rec = nullptr;
     float4* leaf_pm = nullptr;
+    float4* sorted_pm = nullptr;
     float* leaf_rad = nullptr;
     gbh_sim_values* sim = nullptr;
     DevState* st = nullptr;

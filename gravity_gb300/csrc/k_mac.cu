@@ -556,6 +556,9 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
     c->bin = bin0;
     m->num_pairs = recorded;
     *out_count = recorded;
+    // the walks above wrote the in-order position copy for a state that did
+    // not advance: the next compaction gathers
+    MTRY(c, cudaMemsetAsync(&c->st->sorted_valid, 0, 4, c->stream));
     // leave the caller's step parameters in force again
     return upload_step_params(c, *params);
 }

@@ -147,6 +147,8 @@ __global__ __launch_bounds__(MERGE_SORT_THREADS) void k_merge_conflicts(StepBuff
 }
 
 __global__ void k_merge_clear(StepBuffers b) {
+    // merged bodies changed after the walk wrote sorted_pm: the next step gathers
+    if (blockIdx.x == 0 && threadIdx.x == 0 && b.st->merged) b.st->sorted_valid = 0u;
     const uint32_t M = min(b.mq->tail, b.N);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
         const uint2 pr = b.mq->pairs[t];

@@ -83,6 +83,8 @@ __global__ __launch_bounds__(PREP_THREADS) void k_prep_count(StepBuffers b) {
     const uint32_t base = tile * PREP_TILE;
     if (base >= n) return;
     const bool dynamic = b.params->static_or_dynamic == GBH_BOUNDS_DYNAMIC;
+    // positions in index order from the last walk when nothing changed them since
+    const bool sorted = b.st->sorted_valid != 0u;
     float pmin[3], pmax[3], lo[3], hi[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -105,7 +107,7 @@ __global__ __launch_bounds__(PREP_THREADS) void k_prep_count(StepBuffers b) {
         const uint32_t g = base + it * PREP_THREADS + threadIdx.x;
         if (g < n) {
             const uint32_t bi = b.idx_in[g];
-            const float4 pm = ld_pos_mass(b.bodies_in, bi);
+            const float4 pm = sorted ? b.sorted_pm[g] : ld_pos_mass(b.bodies_in, bi);
             if (pm.w == 0.0f) {
                 ++dead;
                 const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -264,6 +266,7 @@ __global__ __launch_bounds__(PREP_THREADS) void k_prep_scatter(StepBuffers b) {
     const uint32_t tile = blockIdx.x;
     const uint32_t base = tile * PREP_TILE;
     if (base >= n_old) return;
+    const bool sorted = st->sorted_valid != 0u;
     __shared__ uint32_t s_hist[SORT_PASSES * SORT_RADIX];
     __shared__ uint32_t s_cnt[PREP_ITEMS][PREP_THREADS / 32];
     __shared__ float s_mn[3], s_mx[3];
@@ -282,7 +285,7 @@ __global__ __launch_bounds__(PREP_THREADS) void k_prep_scatter(StepBuffers b) {
         const uint32_t g = base + it * PREP_THREADS + threadIdx.x;
         const bool in = g < n_old;
         bidx[it] = in ? b.idx_in[g] : 0u;
-        pm[it] = in ? ld_pos_mass(b.bodies_in, bidx[it]) : make_float4(0, 0, 0, 0);
+        pm[it] = in ? (sorted ? b.sorted_pm[g] : ld_pos_mass(b.bodies_in, bidx[it])) : make_float4(0, 0, 0, 0);
         alive[it] = in && pm[it].w != 0.0f;
         const uint32_t bal = __ballot_sync(0xffffffffu, alive[it]);
         wrank[it] = __popc(bal & lanemask_lt());

@@ -186,9 +186,11 @@ __device__ __forceinline__ NodeVals combine(const NodeVals& L, const NodeVals& R
         out.cm.x = (lw * L.cm.x + rw * R.cm.x) / M;
         out.cm.y = (lw * L.cm.y + rw * R.cm.y) / M;
         out.cm.z = (lw * L.cm.z + rw * R.cm.z) / M;
-        out.col.x = (lw * L.col.x + rw * R.col.x) / M;
-        out.col.y = (lw * L.col.y + rw * R.col.y) / M;
-        out.col.z = (lw * L.col.z + rw * R.col.z) / M;
+        // the colour (render-only, compared with a tolerance) by one reciprocal
+        const float inv_m = 1.0f / M;
+        out.col.x = (lw * L.col.x + rw * R.col.x) * inv_m;
+        out.col.y = (lw * L.col.y + rw * R.col.y) * inv_m;
+        out.col.z = (lw * L.col.z + rw * R.col.z) * inv_m;
     } else {
         out.cm.x = (L.cm.x + R.cm.x) * 0.5f;
         out.cm.y = (L.cm.y + R.cm.y) * 0.5f;

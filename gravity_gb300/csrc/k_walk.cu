@@ -49,6 +49,7 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t warp_global = blockIdx.x * WALK_WARPS + w;
     const uint32_t g = warp_global * 32 + lane;
+    if (blockIdx.x == 0 && threadIdx.x == 0) b.st->sorted_valid = 1u;  // the update below fills sorted_pm
     if (warp_global * 32 >= n) return;
     const bool active = g < n;
     const gbh_step_params* P = b.params;
@@ -212,9 +213,9 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     if (b.accel_mag) b.accel_mag[bi] = sqrtf(ax * ax + ay * ay + az * az);
     if (want_pot) b.potential[bi] = pot;
     if (PREC)
-        walk_update_fp64(b, P, sim, bi, pm, vd, ax, ay, az);
+        walk_update_fp64(b, P, sim, g, bi, pm, vd, ax, ay, az);
     else
-        walk_update(b, P, sim, bi, pm, vd, ax, ay, az);
+        walk_update(b, P, sim, g, bi, pm, vd, ax, ay, az);
 }
 
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s) {

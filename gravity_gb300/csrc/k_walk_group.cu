@@ -134,6 +134,9 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     using Cfg = GroupCfg<MODE>;
     typename Cfg::Smem& S = *reinterpret_cast<typename Cfg::Smem*>(smem_raw);
     if (MODE == GM_LEARNED) mac_load_frag(mw, S.frag, S.x);
+    // the updates below fill sorted_pm (the recording walk updates nothing the
+    // step keeps)
+    if (MODE != GM_RECORD && blockIdx.x == 0 && threadIdx.x == 0) b.st->sorted_valid = 1u;
     const float band_lo = (MODE != GM_THETA) ? mw.band[0] : 0.0f;
     const float band_hi = (MODE != GM_THETA) ? mw.band[1] : 0.0f;
     const uint32_t n = b.st->n_new;
@@ -506,9 +509,9 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         if (want_pot) b.potential[bi] = fp;
         const float4 vd = ld_vel_density(b.bodies_in, bi);
         if (PREC)
-            walk_update_fp64(b, P, sim, bi, pm, vd, fx, fy, fz);
+            walk_update_fp64(b, P, sim, gq[q], bi, pm, vd, fx, fy, fz);
         else
-            walk_update(b, P, sim, bi, pm, vd, fx, fy, fz);
+            walk_update(b, P, sim, gq[q], bi, pm, vd, fx, fy, fz);
     }
     __syncwarp();
     }  // groups
