@@ -1,7 +1,7 @@
 // k_walk_group.cu — group walk: one acceptance decision per (body group, node).
 //
 // The reference decides per body (bh_force.comp:57-115).  Here a warp takes
-// one body group, a subtree of at most GBH_GROUP_MAX = 64 bodies (two per
+// one body group, a subtree of at most GBH_GROUP_MAX = 96 bodies (three per
 // lane; k_find_groups), and walks the tree once for all of its bodies:
 //   * candidates come off a per-warp stack 32 at a time, one per lane; each
 //     lane evaluates the acceptance criterion of the group against its node;
@@ -144,7 +144,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t num_groups = b.st->num_groups;
     // groups hold up to GBH_GROUP_MAX bodies, usually fewer: warps loop over
-    // them; lane l holds bodies l and l + 32 of the group
+    // them; lane l holds bodies l, l + 32, l + 64 of the group
     for (uint32_t gi = blockIdx.x * GW_WARPS + w; gi < num_groups; gi += gridDim.x * GW_WARPS) {
     const uint2 grp = b.groups[gi];
     uint32_t gq[GW_BPL];

@@ -66,7 +66,7 @@ extern "C" {
 #define GBH_BOUNDS_DYNAMIC 1u
 /* acceptance criterion of the walk (new in this library) */
 #define GBH_MAC_PLAIN 0u    /* reference rule: (longest AABB side / 2) * invDist < theta, per body */
-#define GBH_MAC_LEARNED 1u  /* learned MLP criterion, one decision per (body group of up to 64, node) */
+#define GBH_MAC_LEARNED 1u  /* learned MLP criterion, one decision per (body group of up to 96, node) */
 #define GBH_MAC_GROUP 2u    /* group theta rule used as the learned criterion's ablation */
 /* precision form (new in this library) */
 #define GBH_PRECISION_FP32 0u     /* reference arithmetic */
