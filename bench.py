@@ -530,7 +530,7 @@ def run_ours(args):
     barrier(dist, local)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        bh.upload_bodies(pin_in)
+        bh.upload_bodies(pin_in, chunk=n)
         bh.step(p_head)
         bh.read_bodies(out=pin_out)
     t1 = time.perf_counter()
