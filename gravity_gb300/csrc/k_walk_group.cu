@@ -16,7 +16,7 @@
 //                    c_g, R_g the centre and half diagonal of the group's box;
 //   GBH_MAC_LEARNED  nodes that pass the group rule at the band's lower theta
 //                    (default 0.25) are accepted, nodes that fail it at its
-//                    upper theta (default 1) are opened (gbh_mac_set_band),
+//                    upper theta (default 4) are opened (gbh_mac_set_band),
 //                    and in between the MLP decides: accept when its predicted
 //                    log10 relative error of the monopole, max over the group,
 //                    is below mac_tolerance (mac_mlp.cuh: features and
@@ -440,7 +440,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                 if (MODE == GM_LEARNED) {
                     // the network decides the band between a rule that is
                     // safe to accept (band_lo, default theta_g = 0.25) and one
-                    // that must open (band_hi, default theta_g = 1): it never
+                    // that must open (band_hi, default theta_g = 4): it never
                     // accepts a node the group reaches
                     const float rho = group_rho(S.geom[w], ng);  // shared copy: fewer live registers
                     kind = rho < band_lo ? 1u : rho < band_hi ? 3u : 2u;

@@ -50,7 +50,7 @@
 // the learned walk's default band: nodes that pass the group rule at
 // MAC_BAND_LO are accepted, nodes that fail it at MAC_BAND_HI opened
 #define MAC_BAND_LO 0.25f
-#define MAC_BAND_HI 1.0f
+#define MAC_BAND_HI 4.0f
 
 struct MacDeviceWeights {
     const uint32_t* frag;  // [MAC_FRAG_WORDS][32]: per-lane fragment words (global)

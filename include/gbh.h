@@ -328,7 +328,7 @@ int gbh_mac_get_weights(gbh_ctx* ctx, float* params, uint32_t count);
  * node < theta x distance from its centre of mass to the group's bounding
  * sphere): nodes that pass the rule at theta_accept are accepted without the
  * network, nodes that fail it at theta_open are opened without it.  Defaults
- * 0.25 and 1.0.  Training pairs are recorded in the same band. */
+ * 0.25 and 4.0.  Training pairs are recorded in the same band. */
 int gbh_mac_set_band(gbh_ctx* ctx, float theta_accept, float theta_open);
 int gbh_mac_get_band(gbh_ctx* ctx, float* theta_accept, float* theta_open);
 /* Sample (body group, node) pairs from the current tree, compute their
