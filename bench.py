@@ -305,7 +305,7 @@ def run_reference(args):
     return 0
 
 
-LEARNED_TAUS = [-3.0, -2.75, -2.6, -2.5, -2.4, -2.3, -2.2, -2.1, -2.0, -1.75, -1.5]
+LEARNED_TAUS = [-3.0, -2.75, -2.6, -2.55, -2.5, -2.45, -2.4, -2.35, -2.3, -2.25, -2.2, -2.15, -2.1, -2.0, -1.9, -1.75, -1.5]
 GROUP_THETAS = [0.4, 0.45, 0.5, 0.55, 0.6, 0.65, 0.7]
 PLAIN_THETAS = [0.3, 0.5, 0.7]
 # DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +

@@ -746,7 +746,7 @@ int gbh_step_profiled(gbh_ctx* c, const gbh_step_params* p, float ms_out[GBH_NUM
     }
     for (int i = 0; i <= GBH_NUM_STAGES; ++i) cudaEventDestroy(ev[i]);
     if (rc) return rc;
-    if ((rc = invalidate_sorted(c))) return rc;
+    // a whole step: the walk's in-order position copy stays current
     after_swap(c, c->params_host.precision_mode == GBH_PRECISION_COMPENSATED);
     return gbh_synchronize(c);
 }

@@ -46,6 +46,7 @@ struct GroupSmem {
     uint32_t stack[GW_WARPS][STACK];
     float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
     uint32_t list_id[GW_WARPS][GW_LIST];
+    float list_rad[GW_WARPS][GW_LIST];  // merge form: the leaf entries' body radii
     // queued band candidates of the learned walk: centre of mass, box and
     // count, box and id, children
     float4 pend_cm[GW_WARPS][GW_QUEUE];
@@ -161,6 +162,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     uint32_t* stk = S.stack[w];
     float4* lcm = S.list_cm[w];
     uint32_t* lid = S.list_id[w];
+    float* lrad = S.list_rad[w];
 
     // group box (inactive slots repeat the first body)
     float4 pmq[GW_BPL];
@@ -254,10 +256,11 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                 for (int q = 0; q < GW_BPL; ++q) {
                     const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
                     if (merging && lj < N && actq[q] && lj != gq[q]) {
-                        // penetration with the leaf's body; a task when
-                        // positive and this body's index is the smaller
-                        const float pen = my_rad[q] + b.leaf_rad[lj] - sqrtf(rx * rx + ry * ry + rz * rz);
-                        if (pen > 0.0f) {
+                        // penetration with the leaf's body (radius kept with
+                        // the entry): a task when the distance is below the
+                        // sum of the radii and this body's index is the smaller
+                        const float rs = my_rad[q] + lrad[j];
+                        if (rx * rx + ry * ry + rz * rz < rs * rs) {
                             const uint32_t bi = b.idx_in[gq[q]], oi = b.idx_in[lj];
                             if (bi < oi) {
                                 const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
@@ -338,6 +341,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             else
                 lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
             lid[pos] = id;
+            if (merging) lrad[pos] = id < N ? b.leaf_rad[id] : 0.0f;
         }
         ln += __popc(bl);
         if (kind == 2) {
@@ -355,6 +359,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             if (lane < ln) {  // move the remaining entries to the front
                 lcm[lane] = lcm[32 + lane];
                 lid[lane] = lid[32 + lane];
+                if (merging) lrad[lane] = lrad[32 + lane];
             }
             __syncwarp();
         }
