@@ -7,7 +7,7 @@ Workload (default): 16,777,216 bodies, 70% Plummer (a=1) + 30% uniform in
 bounds, no merges; seeded synthetic input (seed 3).
 
 Before timing (untimed): the MLP is trained on this state on the GPU
-(gbh_mac_generate + gbh_mac_train), the direct-sum judge takes 4096 sampled
+(gbh_mac_generate + gbh_mac_train), the direct sum over a seeded sample of 4096
 bodies, and the learned walk's tolerance is the one with the fewest
 interactions whose p99 error is at or below the plain theta = 0.5 walk's.
 
@@ -423,9 +423,9 @@ def run_ours(args):
             losses = bh.mac_train(epochs=args.mac_epochs, batch=16384, lr=3e-3, seed=0)
             calib["training"] = {"pairs": pairs, "epochs": args.mac_epochs, "loss_first": float(losses[0]),
                                  "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
-        judge = accuracy.Judge(bh, p_plain, count=4096, seed=2)
-        ref = {th: accuracy.evaluate(bh, judge, plain(th)) for th in PLAIN_THETAS}
-        head = accuracy.evaluate(bh, judge, p_plain)
+        ref_sample = accuracy.DirectSumSample(bh, p_plain, count=4096, seed=2)
+        ref = {th: accuracy.evaluate(bh, ref_sample, plain(th)) for th in PLAIN_THETAS}
+        head = accuracy.evaluate(bh, ref_sample, p_plain)
         target = head["p99"]
         calib["plain"] = {f"{th:g}": {k: r[k] for k in ("median", "p90", "p99", "max", "interactions")}
                           for th, r in ref.items()}
@@ -433,10 +433,10 @@ def run_ours(args):
         calib["p99_target"] = target
         if args.mac_tolerance is not None:
             tau = args.mac_tolerance
-            r = accuracy.evaluate(bh, judge, learned(tau))
+            r = accuracy.evaluate(bh, ref_sample, learned(tau))
             best_l = (tau, r)
         else:
-            best_l, res_l = accuracy.match_p99(bh, judge, learned, LEARNED_TAUS, target)
+            best_l, res_l = accuracy.match_p99(bh, ref_sample, learned, LEARNED_TAUS, target)
             calib["learned_sweep"] = [{k: r[k] for k in ("setting", "p99", "interactions", "mac_evaluations")}
                                       for r in res_l]
         if best_l is None:
@@ -447,7 +447,7 @@ def run_ours(args):
         p_head = learned(best_l[0])
         mac_name = "learned"
         if not args.no_compare:
-            best_g, res_g = accuracy.match_p99(bh, judge, group, GROUP_THETAS, target)
+            best_g, res_g = accuracy.match_p99(bh, ref_sample, group, GROUP_THETAS, target)
             if best_g is not None:
                 calib["group"] = {k: best_g[1][k] for k in ("median", "p90", "p99", "max", "interactions")}
                 calib["group"]["theta"] = best_g[0]

@@ -1,7 +1,7 @@
-"""Acceleration error of a walk against the direct-sum judge, and matching of
+"""Acceleration error of a walk against the direct-sum reference, and matching of
 acceptance settings at equal p99 error.
 
-The judge (gbh_direct_sum) sums every body's pull on a seeded sample of bodies
+The reference (gbh_direct_sum) sums every body's pull on a seeded sample of bodies
 with FP32 terms and compensated sums (within ~1e-6 of an FP64 sum).  Errors
 are |a_walk - a_direct| / |a_direct| per sampled body.
 """
@@ -23,7 +23,7 @@ def live_ids(sim) -> np.ndarray:
     return np.nonzero(b["pos_mass"][:, 3] != 0)[0].astype(np.uint32)
 
 
-class Judge:
+class DirectSumSample:
     """Direct-sum reference accelerations of a fixed sample of the current state."""
 
     def __init__(self, sim, params: abi.StepParams, count: int = 4096, seed: int = 0):
@@ -44,24 +44,24 @@ def summarize(err: np.ndarray) -> dict:
     }
 
 
-def evaluate(sim, judge: Judge, params: abi.StepParams) -> dict:
+def evaluate(sim, ref_sample: DirectSumSample, params: abi.StepParams) -> dict:
     """Error summary and interactions of one walk of the current state."""
     acc = sim.evaluate_walk(params)
     s = sim.read_stats()
-    out = summarize(judge.errors(acc))
+    out = summarize(ref_sample.errors(acc))
     out["interactions"] = int(s.interactions)
     out["mac_evaluations"] = int(s.mac_evaluations)
     return out
 
 
-def match_p99(sim, judge: Judge, make_params, grid, target_p99: float):
+def match_p99(sim, ref_sample: DirectSumSample, make_params, grid, target_p99: float):
     """The setting of `grid` (ordered from accurate to aggressive) with the
     fewest interactions whose p99 error stays at or below `target_p99`.
     Returns (value, result dict, all results)."""
     results = []
     best = None
     for v in grid:
-        r = evaluate(sim, judge, make_params(v))
+        r = evaluate(sim, ref_sample, make_params(v))
         r["setting"] = float(v)
         results.append(r)
         if r["p99"] <= target_p99 and (best is None or r["interactions"] < best[1]["interactions"]):

@@ -203,7 +203,7 @@ class BarnesHut:
         a = np.ascontiguousarray(keys, dtype=np.uint64)
         self._chk(lib().gbh_write_morton(self._h, _ptr(a), len(a), offset))
 
-    # ---- accuracy judge --------------------------------------------------------
+    # ---- accuracy reference --------------------------------------------------------
     def direct_sum(self, params: abi.StepParams, sample: np.ndarray) -> np.ndarray:
         s = np.ascontiguousarray(sample, dtype=np.uint32)
         out = np.zeros((len(s), 3), dtype=np.float64)

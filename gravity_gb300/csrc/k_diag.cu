@@ -1,8 +1,8 @@
-// k_diag.cu — the accuracy judge (direct-sum accelerations of sampled bodies),
+// k_diag.cu — the accuracy reference (direct-sum accelerations of sampled bodies),
 // the FP64 diagnostics of conserved quantities, and the FP64 positions of the
 // precision form.
 //
-// The reference has no accuracy check.  The judge sums G m_j r / (r.r + eps^2)^1.5
+// The reference has no accuracy check.  The direct sum adds G m_j r / (r.r + eps^2)^1.5
 // over every live body j != i for a sample of bodies i.  Each term is computed
 // in FP32 (the positions are FP32, so r = x_j - x_i carries one rounding) and
 // the sums are carried in double-float (TwoSum compensation), so the result
@@ -87,7 +87,7 @@ void launch_direct_sum(const gbh_body* bodies, uint32_t nb, const uint32_t* samp
 // ---------------------------------------------------------------------------
 // FP64 direct sum of the precision form: positions from the FP64 copy, terms
 // and sums in FP64 (the GB300 runs FP64 at a fraction of the FP32 rate; the
-// judge samples a few thousand bodies).
+// reference samples a few thousand bodies).
 __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __restrict__ pos64,
                                                              const gbh_body* __restrict__ bodies, uint32_t nb,
                                                              const uint32_t* __restrict__ sample, uint32_t count,

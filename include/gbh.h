@@ -308,7 +308,7 @@ int gbh_stage_swap(gbh_ctx* ctx);
  * fill, walk, merge, swap). */
 int gbh_step_profiled(gbh_ctx* ctx, const gbh_step_params* params, float ms_out[GBH_NUM_STAGES]);
 
-/* ---- accuracy judge -------------------------------------------------------
+/* ---- accuracy reference -------------------------------------------------------
  * Direct-sum accelerations for `count` sampled body indices against every live
  * body of the current state (terms in FP32, sums compensated in double-float).
  * out: double[3*count].  Uses G, softening from `params`. */

@@ -1002,7 +1002,7 @@ int orc_write_morton(orc_ctx* c, const uint64_t* host, uint32_t count, uint32_t 
     return GBH_OK;
 }
 
-/* ---- FP64 direct sum (the accuracy judge) ----------------------------------- */
+/* ---- FP64 direct sum (the accuracy reference) ----------------------------------- */
 int orc_direct_sum_fp64(const gbh_body* bodies, uint32_t n, const uint32_t* sample, uint32_t count, double G,
                         double soft, double* out) {
     if (!bodies || !sample || !out) return GBH_ERR_INVALID;

@@ -43,10 +43,10 @@ def test_group_walk_runs_and_is_accurate(gbh_lib):
     bodies = ic.plummer(65536, seed=2)
     sim = _sim(bodies)
     p = abi.step_params(theta=0.5, softening=1e-4)
-    judge = accuracy.Judge(sim, p, count=2048, seed=1)
-    plain = accuracy.evaluate(sim, judge, p)
-    g3 = accuracy.evaluate(sim, judge, abi.step_params(theta=0.3, softening=1e-4, mac=abi.MAC_GROUP))
-    g8 = accuracy.evaluate(sim, judge, abi.step_params(theta=0.8, softening=1e-4, mac=abi.MAC_GROUP))
+    ref_sample = accuracy.DirectSumSample(sim, p, count=2048, seed=1)
+    plain = accuracy.evaluate(sim, ref_sample, p)
+    g3 = accuracy.evaluate(sim, ref_sample, abi.step_params(theta=0.3, softening=1e-4, mac=abi.MAC_GROUP))
+    g8 = accuracy.evaluate(sim, ref_sample, abi.step_params(theta=0.8, softening=1e-4, mac=abi.MAC_GROUP))
     assert sim.read_stats().error_word == 0
     assert g3["p99"] < g8["p99"]
     assert g3["interactions"] > g8["interactions"]
@@ -107,13 +107,13 @@ def test_learned_mac_pipeline_and_gain(gbh_lib):
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.6 * losses[0], losses
     # the trained criterion against the group theta rule at the plain rule's p99
-    judge = accuracy.Judge(sim, p, count=2048, seed=2)
-    target = accuracy.evaluate(sim, judge, p)["p99"]
+    ref_sample = accuracy.DirectSumSample(sim, p, count=2048, seed=2)
+    target = accuracy.evaluate(sim, ref_sample, p)["p99"]
     best_l, res_l = accuracy.match_p99(
-        sim, judge, lambda t: abi.step_params(theta=0.5, softening=soft, mac=abi.MAC_LEARNED, mac_tolerance=t),
+        sim, ref_sample, lambda t: abi.step_params(theta=0.5, softening=soft, mac=abi.MAC_LEARNED, mac_tolerance=t),
         [-4.0, -3.5, -3.0, -2.75, -2.5, -2.25, -2.0, -1.75, -1.5, -1.25, -1.0], target)
     best_g, res_g = accuracy.match_p99(
-        sim, judge, lambda t: abi.step_params(theta=t, softening=soft, mac=abi.MAC_GROUP),
+        sim, ref_sample, lambda t: abi.step_params(theta=t, softening=soft, mac=abi.MAC_GROUP),
         [0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.2], target)
     assert best_l is not None and best_g is not None, (res_l, res_g)
     assert best_l[1]["interactions"] < best_g[1]["interactions"], (best_l, best_g)

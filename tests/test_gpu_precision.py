@@ -1,6 +1,6 @@
 """The precision form (GBH_PRECISION_COMPENSATED): FP64 drift, walk offsets
 from the FP32 position plus its FP32 residual with compensated near-field
-sums, the FP64 judge and the FP64 diagnostics, against FP64 numpy."""
+sums, the FP64 direct sum and the FP64 diagnostics, against FP64 numpy."""
 import numpy as np
 import pytest
 
