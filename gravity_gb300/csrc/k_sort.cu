@@ -51,13 +51,44 @@ struct SortSmem {
     uint32_t vals[SORT_TILE];
 };
 
-__global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, uint32_t pass, const uint64_t* __restrict__ kin,
+// Warp-level stable ranking of the items, item rounds in slot order: lanes
+// with the same digit from one ballot per digit bit (BITS = 9 in a partial
+// tile, whose out-of-range slots carry the sentinel digit 256); the digit's
+// leader reserves the group's ranks with a shared-memory atomic.  A warp's
+// shared memory atomics take effect in program order, so items stay in slot
+// order.
+template <uint32_t SHIFT, int BITS>
+__device__ __forceinline__ void rank_items(const uint64_t (&key)[SORT_ITEMS], uint32_t (&rank)[SORT_ITEMS],
+                                           uint32_t* warp_hist, uint32_t lane, uint32_t seg, uint32_t n) {
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        uint32_t dig = (uint32_t)(key[i] >> SHIFT) & 0xFFu;
+        if (BITS > 8 && seg + i * 32 + lane >= n) dig = SORT_RADIX;
+        uint32_t peers = 0xffffffffu;
+#pragma unroll
+        for (int bit = 0; bit < BITS; ++bit) {
+            const bool on = (dig >> bit) & 1u;
+            const uint32_t m = __ballot_sync(0xffffffffu, on);
+            peers &= on ? m : ~m;
+        }
+        const uint32_t leader = __ffs(peers) - 1;
+        const uint32_t before = __popc(peers & lanemask_lt());
+        uint32_t prev = 0;
+        if (lane == leader) prev = atomicAdd(&warp_hist[dig], (uint32_t)__popc(peers));
+        rank[i] = __shfl_sync(0xffffffffu, prev, leader) + before;
+    }
+}
+
+// One kernel instance per pass: the digit's bit offset is a constant.
+template <uint32_t PASS>
+__global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, const uint64_t* __restrict__ kin,
                                                                const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                                                uint32_t* __restrict__ vout) {
+    constexpr uint32_t pass = PASS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem& S = *reinterpret_cast<SortSmem*>(smem_raw);
     const uint32_t n = b.st->n_new;
-    const uint32_t shift = SORT_BITS * pass;
+    constexpr uint32_t shift = SORT_BITS * PASS;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     if (threadIdx.x == 0) S.tile = atomicAdd(&b.st->sort_tiles[pass], 1u);
     for (uint32_t i = threadIdx.x; i < (SORT_THREADS / 32) * (SORT_RADIX + 1); i += SORT_THREADS)
@@ -70,41 +101,30 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, ui
 
     // load: warp w owns slots [base + w*32*ITEMS, +32*ITEMS), item i of lane l at +i*32+l
     const uint32_t seg = base + w * 32 * SORT_ITEMS;
+    const bool full = base + SORT_TILE <= n;  // uniform over the block
     uint64_t key[SORT_ITEMS];
     uint32_t val[SORT_ITEMS];
     uint32_t rank[SORT_ITEMS];
+    if (full) {
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; ++i) {
-        const uint32_t pos = seg + i * 32 + lane;
-        if (pos < n) {
-            key[i] = kin[pos];
-            val[i] = vin[pos];
-        } else {
-            key[i] = ~0ull;
-            val[i] = 0;
+        for (int i = 0; i < SORT_ITEMS; ++i) {
+            key[i] = kin[seg + i * 32 + lane];
+            val[i] = vin[seg + i * 32 + lane];
         }
-    }
-    // warp-level stable ranking, item rounds in slot order
+        rank_items<shift, 8>(key, rank, S.warp_hist[w], lane, seg, n);
+    } else {
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; ++i) {
-        const uint32_t pos = seg + i * 32 + lane;
-        const uint32_t dig = pos < n ? (uint32_t)((key[i] >> shift) & 0xFF) : SORT_RADIX;
-        // lanes with the same digit (9 bits: 256 is the sentinel of
-        // out-of-range slots), from one ballot per bit
-        uint32_t peers = 0xffffffffu;
-#pragma unroll
-        for (int bit = 0; bit < 9; ++bit) {
-            const bool on = (dig >> bit) & 1u;
-            const uint32_t m = __ballot_sync(0xffffffffu, on);
-            peers &= on ? m : ~m;
+        for (int i = 0; i < SORT_ITEMS; ++i) {
+            const uint32_t pos = seg + i * 32 + lane;
+            if (pos < n) {
+                key[i] = kin[pos];
+                val[i] = vin[pos];
+            } else {
+                key[i] = ~0ull;
+                val[i] = 0;
+            }
         }
-        const uint32_t leader = __ffs(peers) - 1;
-        const uint32_t before = __popc(peers & lanemask_lt());
-        // the digit's leader reserves the group's ranks; a warp's shared
-        // memory atomics take effect in program order, so items stay in slot order
-        uint32_t prev = 0;
-        if (lane == leader) prev = atomicAdd(&S.warp_hist[w][dig], (uint32_t)__popc(peers));
-        rank[i] = __shfl_sync(0xffffffffu, prev, leader) + before;
+        rank_items<shift, 9>(key, rank, S.warp_hist[w], lane, seg, n);
     }
     __syncthreads();
     // thread d: exclusive prefix of digit d over warps, tile total
@@ -169,8 +189,8 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, ui
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t pos = seg + i * 32 + lane;
         if (pos < n) {
-            const uint32_t dig = (uint32_t)((key[i] >> shift) & 0xFF);
-            const uint32_t local = S.block_excl[dig] + S.warp_hist[w][dig] + rank[i];
+            const uint32_t dg = (uint32_t)(key[i] >> shift) & 0xFFu;
+            const uint32_t local = S.block_excl[dg] + S.warp_hist[w][dg] + rank[i];
             S.keys[local] = key[i];
             S.vals[local] = val[i];
         }
@@ -180,8 +200,7 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, ui
     bool bad = false;
     for (uint32_t j = threadIdx.x; j < valid; j += SORT_THREADS) {
         const uint64_t k = S.keys[j];
-        const uint32_t dig = (uint32_t)((k >> shift) & 0xFF);
-        const uint32_t dst = S.delta[dig] + j;
+        const uint32_t dst = S.delta[(uint32_t)(k >> shift) & 0xFFu] + j;
         if (dst < n) {  // holds whenever the digit histograms describe these keys
             kout[dst] = k;
             vout[dst] = S.vals[j];
@@ -193,7 +212,14 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, ui
 }
 
 void sort_setup() {
-    cudaFuncSetAttribute(k_sort_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
+    cudaFuncSetAttribute(k_sort_pass<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
 }
 
 void launch_sort(const StepBuffers& b, cudaStream_t s) {
@@ -205,8 +231,12 @@ void launch_sort(const StepBuffers& b, cudaStream_t s) {
     const uint32_t* vin = b.idx_in;
     uint64_t* kt = b.keys_out;
     uint32_t* vt = b.idx_out;
+    static_assert(SORT_PASSES == 8, "one kernel instance per pass");
+    void (*const kernels[SORT_PASSES])(StepBuffers, const uint64_t*, const uint32_t*, uint64_t*, uint32_t*) = {
+        k_sort_pass<0>, k_sort_pass<1>, k_sort_pass<2>, k_sort_pass<3>,
+        k_sort_pass<4>, k_sort_pass<5>, k_sort_pass<6>, k_sort_pass<7>};
     for (uint32_t p = 0; p < SORT_PASSES; ++p) {
-        k_sort_pass<<<b.sort_tiles_cap, SORT_THREADS, smem, s>>>(b, p, kin, vin, kt, vt);
+        kernels[p]<<<b.sort_tiles_cap, SORT_THREADS, smem, s>>>(b, kin, vin, kt, vt);
         const uint64_t* nk = kt;
         const uint32_t* nv = vt;
         kt = const_cast<uint64_t*>(kin);

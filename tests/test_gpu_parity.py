@@ -46,7 +46,7 @@ def test_prepare_bit_exact(gbh_lib, oracle_mod, n, dead, nans, outl, dynamic):
         assert np.array_equal(g.read_bodies(w).view(np.uint32), o.read_bodies(w).view(np.uint32))
 
 
-@pytest.mark.parametrize("n", [2, 3, 1000, 4096, 70000, 262144])
+@pytest.mark.parametrize("n", [2, 3, 1000, 4096, 16381, 70000, 262144])
 def test_sort_permutation_bit_exact(gbh_lib, oracle_mod, n):
     b = plummer_case(n, seed=7 + n)
     g, o = make_pair(oracle_mod, BarnesHut, b, bounds_of(b))

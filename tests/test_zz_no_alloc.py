@@ -56,6 +56,27 @@ def test_sort_pairs_noalloc_matches_stage_sort(gbh_lib):
         assert np.array_equal(kin.cpu().numpy().view(np.uint64), keys)
 
 
+def test_sort_pairs_noalloc_unaligned_buffers(gbh_lib):
+    # output buffers that start off a 16-byte boundary (views one element
+    # into larger tensors) and a ragged last tile of odd length
+    torch = pytest.importorskip("torch")
+    stream = torch.cuda.current_stream()
+    n = 3 * 4096 + 1001  # a ragged last tile of odd length
+    keys, idx, want_k, want_v = _unsorted_and_sorted(n, 8)
+    kin = torch.from_numpy(keys.view(np.int64)).cuda()
+    vin = torch.from_numpy(idx.view(np.int32)).cuda()
+    kout = torch.empty(n + 1, dtype=torch.int64, device="cuda")[1:]
+    vout = torch.empty(n + 1, dtype=torch.int32, device="cuda")[1:]
+    assert kout.data_ptr() % 16 and vout.data_ptr() % 16
+    torch.cuda.synchronize()
+    rc = gbh_lib.gbh_sort_pairs_noalloc(
+        C.c_void_p(kin.data_ptr()), C.c_void_p(vin.data_ptr()), C.c_void_p(kout.data_ptr()),
+        C.c_void_p(vout.data_ptr()), n, C.c_void_p(stream.cuda_stream))
+    assert rc == abi.GBH_OK
+    assert np.array_equal(kout.cpu().numpy().view(np.uint64), want_k)
+    assert np.array_equal(vout.cpu().numpy().view(np.uint32), want_v)
+
+
 def test_sort_pairs_noalloc_rejects_oversize(gbh_lib):
     rc = gbh_lib.gbh_sort_pairs_noalloc(C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), C.c_void_p(1),
                                         (1 << 20) + 1, None)
