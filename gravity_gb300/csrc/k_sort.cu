@@ -20,6 +20,9 @@
 #define LB_FLAG_INC 0x80000000u
 #define LB_COUNT_MASK 0x3FFFFFFFu
 #define LB_SPIN_LIMIT (1u << 22)
+#ifndef LB_WINDOW
+#define LB_WINDOW 4
+#endif
 
 __global__ void k_sort_scan(StepBuffers b) {
     // one block per pass: exclusive scan of the 256 digit counts
@@ -158,33 +161,10 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
         S.block_excl[d] = off + x - total;
         if (d == 0) S.block_excl[SORT_RADIX] = 0;
     }
-    // decoupled look-back for digit d
-    uint32_t prefix = 0;
-    if (tile > 0) {
-        int32_t j = (int32_t)tile - 1;
-        uint32_t spins = 0;
-        while (j >= 0) {
-            const uint32_t v = *(volatile uint32_t*)(lb + (size_t)j * SORT_RADIX + d);
-            if (v & LB_FLAG_INC) {
-                prefix += v & LB_COUNT_MASK;
-                break;
-            }
-            if (v & LB_FLAG_AGG) {
-                prefix += v & LB_COUNT_MASK;
-                --j;
-                continue;
-            }
-            if (++spins > LB_SPIN_LIMIT) {
-                set_error(b.st, GBH_DEVERR_SORT_LOOKBACK);
-                break;
-            }
-            __nanosleep(20);
-        }
-        *my = LB_FLAG_INC | (prefix + total);
-    }
-    S.delta[d] = b.bucket_base[pass * SORT_RADIX + d] + prefix - S.block_excl[d];
     __syncthreads();
-    // stage digit-ordered in shared memory
+    // stage digit-ordered in shared memory (tile-local offsets only), before
+    // the look-back: the items leave the registers, and the predecessors
+    // have longer to publish their inclusive counts
 #pragma unroll
     for (int i = 0; i < SORT_ITEMS; ++i) {
         const uint32_t pos = seg + i * 32 + lane;
@@ -195,6 +175,50 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
             S.vals[local] = val[i];
         }
     }
+    // decoupled look-back for digit d, LB_WINDOW predecessors per round
+    // trip; tile 0 always publishes an inclusive count, so the walk ends
+    // there at the latest
+    uint32_t prefix = 0;
+    if (tile > 0) {
+        int32_t j = (int32_t)tile - 1;
+        uint32_t spins = 0;
+        while (true) {
+            uint32_t v[LB_WINDOW];
+#pragma unroll
+            for (int k = 0; k < LB_WINDOW; ++k)
+                v[k] = (j - k >= 0) ? *(volatile uint32_t*)(lb + (size_t)(j - k) * SORT_RADIX + d) : LB_FLAG_INC;
+            // aggregates add and continue, an inclusive count adds and ends
+            // the walk, a word not yet published ends the round
+            uint32_t add = 0, used = 0, state = 0;  // state 1: inclusive found, 2: not yet published
+#pragma unroll
+            for (int k = 0; k < LB_WINDOW; ++k) {
+                if (state == 0) {
+                    const uint32_t xv = v[k];
+                    if (xv & LB_FLAG_INC) {
+                        add += xv & LB_COUNT_MASK;
+                        state = 1;
+                    } else if (xv & LB_FLAG_AGG) {
+                        add += xv & LB_COUNT_MASK;
+                        ++used;
+                    } else {
+                        state = 2;
+                    }
+                }
+            }
+            prefix += add;
+            if (state == 1) break;
+            j -= (int32_t)used;
+            if (used == 0) {
+                if (++spins > LB_SPIN_LIMIT) {
+                    set_error(b.st, GBH_DEVERR_SORT_LOOKBACK);
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        *my = LB_FLAG_INC | (prefix + total);
+    }
+    S.delta[d] = b.bucket_base[pass * SORT_RADIX + d] + prefix - S.block_excl[d];
     __syncthreads();
     const uint32_t valid = min((uint32_t)SORT_TILE, n - base);
     bool bad = false;
