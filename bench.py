@@ -436,7 +436,7 @@ def run_ours(args):
             r = accuracy.evaluate(bh, ref_sample, learned(tau))
             best_l = (tau, r)
         else:
-            best_l, res_l = accuracy.match_p99(bh, ref_sample, learned, LEARNED_TAUS, target)
+            best_l, res_l = accuracy.match_p99(bh, ref_sample, learned, LEARNED_TAUS, target, refine=3)
             calib["learned_sweep"] = [{k: r[k] for k in ("setting", "p99", "interactions", "mac_evaluations")}
                                       for r in res_l]
         if best_l is None:
@@ -447,7 +447,7 @@ def run_ours(args):
         p_head = learned(best_l[0])
         mac_name = "learned"
         if not args.no_compare:
-            best_g, res_g = accuracy.match_p99(bh, ref_sample, group, GROUP_THETAS, target)
+            best_g, res_g = accuracy.match_p99(bh, ref_sample, group, GROUP_THETAS, target, refine=3)
             if best_g is not None:
                 calib["group"] = {k: best_g[1][k] for k in ("median", "p90", "p99", "max", "interactions")}
                 calib["group"]["theta"] = best_g[0]

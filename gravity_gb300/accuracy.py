@@ -54,16 +54,36 @@ def evaluate(sim, ref_sample: DirectSumSample, params: abi.StepParams) -> dict:
     return out
 
 
-def match_p99(sim, ref_sample: DirectSumSample, make_params, grid, target_p99: float):
+def match_p99(sim, ref_sample: DirectSumSample, make_params, grid, target_p99: float, refine: int = 0):
     """The setting of `grid` (ordered from accurate to aggressive) with the
     fewest interactions whose p99 error stays at or below `target_p99`.
-    Returns (value, result dict, all results)."""
+    With `refine` > 0, when the grid's next (more aggressive) setting after
+    that one misses the target, `refine` bisection steps between the two look
+    for a setting closer to the target.  Returns (value, result dict, all
+    results)."""
     results = []
     best = None
-    for v in grid:
+
+    def run(v):
+        nonlocal best
         r = evaluate(sim, ref_sample, make_params(v))
         r["setting"] = float(v)
         results.append(r)
         if r["p99"] <= target_p99 and (best is None or r["interactions"] < best[1]["interactions"]):
             best = (float(v), r)
+        return r
+
+    for v in grid:
+        run(v)
+    if refine and best is not None:
+        settings = [float(v) for v in grid]
+        i = settings.index(best[0])
+        if i + 1 < len(settings) and results[i + 1]["p99"] > target_p99:
+            lo, hi = settings[i], settings[i + 1]
+            for _ in range(refine):
+                mid = 0.5 * (lo + hi)
+                if run(mid)["p99"] <= target_p99:
+                    lo = mid
+                else:
+                    hi = mid
     return best, results

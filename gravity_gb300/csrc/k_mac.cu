@@ -510,10 +510,13 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
     MTRY(c, cudaGetLastError());
     // 2. record candidate pairs from a conservative and an aggressive group
     //    walk (half of the budget each), so that the pairs cover what both
-    //    strict and loose criteria meet
-    MTRY(c, cudaMemsetAsync(m->count, 0, 4, c->stream));
+    //    strict and loose criteria meet.  A walk meets far more band
+    //    candidates than the budget holds: a count pass first, then a hashed
+    //    subset of (group, node) sized to about 95% of the budget, so the
+    //    pairs come from every group rather than from the first ones to run.
     launch_find_groups(ctx_buffers(c), c->stream);
     const float thetas[2] = {0.25f, 0.6f};
+    uint32_t start = 0;
     for (int r = 0; r < 2; ++r) {
         p.mac_mode = GBH_MAC_GROUP;
         p.theta = thetas[r];
@@ -524,21 +527,33 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
         mw.rec_count = m->count;
         mw.rec_pairs = m->pairs;
         mw.rec_feats = m->feats;
-        mw.rec_cap = r == 0 ? max_pairs / 2 : max_pairs;
         mw.rec_max_bodies = 0xFFFFFFFFu;
-        mw.rec_keep = 1024;
         mw.rec_seed = (uint32_t)(seed ^ (seed >> 32)) + 0x51ED27u * r;
-        // the group walk writes the output bodies; they are discarded (no swap)
+        const uint32_t cap = r == 0 ? max_pairs / 2 : max_pairs;
+        const uint32_t budget = cap - start;
+        // count pass over a 1/16 hashed subset (nothing stored; the 32-bit
+        // counter stays far from wrapping); the group walk writes the output
+        // bodies, which are discarded (no swap)
+        uint32_t met = 0;
+        MTRY(c, cudaMemsetAsync(m->count, 0, 4, c->stream));
+        mw.rec_cap = 0;
+        mw.rec_keep = 0x0FFFFFFFu;
         launch_walk_group_record(ctx_buffers(c), mw, c->stream);
         MTRY(c, cudaGetLastError());
-        if (r == 0) {
-            // the second walk appends after the first one's (capped) pairs
-            uint32_t first = 0;
-            MTRY(c, cudaMemcpyAsync(&first, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
-            MTRY(c, cudaStreamSynchronize(c->stream));
-            first = first < max_pairs / 2 ? first : max_pairs / 2;
-            MTRY(c, cudaMemcpyAsync(m->count, &first, 4, cudaMemcpyHostToDevice, c->stream));
-        }
+        MTRY(c, cudaMemcpyAsync(&met, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
+        MTRY(c, cudaStreamSynchronize(c->stream));
+        const double frac = met ? 0.95 * (double)budget / (16.0 * (double)met) : 1.0;
+        mw.rec_keep = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
+        // record pass, appending after the pairs kept so far
+        MTRY(c, cudaMemcpyAsync(m->count, &start, 4, cudaMemcpyHostToDevice, c->stream));
+        mw.rec_cap = cap;
+        launch_walk_group_record(ctx_buffers(c), mw, c->stream);
+        MTRY(c, cudaGetLastError());
+        uint32_t end = 0;
+        MTRY(c, cudaMemcpyAsync(&end, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
+        MTRY(c, cudaStreamSynchronize(c->stream));
+        start = end < cap ? end : cap;
+        MTRY(c, cudaMemcpyAsync(m->count, &start, 4, cudaMemcpyHostToDevice, c->stream));
     }
     uint32_t recorded = 0;
     MTRY(c, cudaMemcpyAsync(&recorded, m->count, 4, cudaMemcpyDeviceToHost, c->stream));

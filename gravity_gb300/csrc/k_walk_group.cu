@@ -453,7 +453,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                     kind = group_theta_accept(gg, ng, theta) ? 1 : 2;
                     // training pairs: the band the network decides (see GM_LEARNED)
                     if (MODE == GM_RECORD && ng.count <= mw.rec_max_bodies &&
-                        (hash32(id ^ hash32(gi + mw.rec_seed)) & 1023u) < mw.rec_keep &&
+                        hash32(id ^ hash32(gi + mw.rec_seed)) <= mw.rec_keep &&
                         group_rho(gg, ng) < band_hi && !(group_rho(gg, ng) < band_lo)) {
                         const uint32_t slot = atomicAdd(mw.rec_count, 1u);
                         if (slot < mw.rec_cap) {

@@ -64,7 +64,7 @@ struct MacDeviceWeights {
     float* rec_feats;      // [cap][MAC_FEATURES]
     uint32_t rec_cap;
     uint32_t rec_max_bodies;  // only nodes with at most this many bodies
-    uint32_t rec_keep;        // keep a pair when hash % 1024 < rec_keep
+    uint32_t rec_keep;        // keep a pair when its 32-bit hash <= rec_keep (0xFFFFFFFF: all)
     uint32_t rec_seed;
 };
 
