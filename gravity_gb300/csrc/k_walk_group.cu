@@ -47,6 +47,11 @@ struct GroupSmem {
     float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
     uint32_t list_id[GW_WARPS][GW_LIST];
     float list_rad[GW_WARPS][GW_LIST];  // merge form: the leaf entries' body radii
+    // merge form: each group body's radius and task counter (slot q * 32 +
+    // lane), the group's largest radius
+    float body_rad[GW_WARPS][GBH_GROUP_MAX];
+    uint32_t body_seq[GW_WARPS][GBH_GROUP_MAX];
+    float grp_rad[GW_WARPS];
     // queued band candidates of the learned walk: centre of mass, box and
     // count, box and id, children
     float4 pend_cm[GW_WARPS][GW_QUEUE];
@@ -218,12 +223,23 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
     constexpr bool merging = FORM == FORM_MERGE;
-    float my_rad[GW_BPL];
-    uint32_t seq[GW_BPL];
+    // the merge state lives in shared memory: the tests are rare (screened)
+    float* my_rad = S.body_rad[w];
+    uint32_t* seq = S.body_seq[w];
+    if (merging) {
+        float gr = 0.0f;
 #pragma unroll
-    for (int q = 0; q < GW_BPL; ++q) {
-        my_rad[q] = (merging && actq[q]) ? b.leaf_rad[gq[q]] : 0.0f;
-        seq[q] = 0;
+        for (int q = 0; q < GW_BPL; ++q) {
+            const float r = actq[q] ? b.leaf_rad[gq[q]] : 0.0f;
+            my_rad[q * 32 + lane] = r;
+            seq[q * 32 + lane] = 0;
+            gr = fmaxf(gr, r);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) gr = fmaxf(gr, __shfl_xor_sync(0xffffffffu, gr, o));
+        __syncwarp();
+        if (lane == 0) S.grp_rad[w] = gr;
+        __syncwarp();
     }
     float ax[GW_BPL], ay[GW_BPL], az[GW_BPL], pot[GW_BPL];
     float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], np_[GW_BPL];  // PREC: leaf terms (Kahan)
@@ -244,8 +260,27 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     // softening of at least 1e-20 a body's own entry adds exactly zero (its
     // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
     const bool self_check = !(soft >= 1e-20f);
+    // penetration of group body q with the leaf entry j (body id lj, radius
+    // kept with the entry): a task when the distance is below the sum of the
+    // radii and this body's index is the smaller (bh_force.comp:109-112)
+    auto merge_test = [&](int q, uint32_t lj, float rx, float ry, float rz, float lr) {
+        if (lj < N && actq[q] && lj != gq[q]) {
+            const float rs = my_rad[q * 32 + lane] + lr;
+            if (rx * rx + ry * ry + rz * rz < rs * rs) {
+                const uint32_t bi = b.idx_in[gq[q]], oi = b.idx_in[lj];
+                if (bi < oi) {
+                    const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
+                    if (slot < N) {
+                        b.mq->pairs[slot] = make_uint2(bi, oi);
+                        b.mkeys[slot] = ((unsigned long long)gq[q] << 32) | seq[q * 32 + lane];
+                    }
+                    ++seq[q * 32 + lane];
+                }
+            }
+        }
+    };
     auto flush = [&](uint32_t cnt) {
-        if (PREC || want_pot || merging) {
+        if (PREC || want_pot) {
             // the general loop: leaf terms apart (PREC), potential, self
             // check, merge tasks
 #pragma unroll 2
@@ -255,23 +290,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
 #pragma unroll
                 for (int q = 0; q < GW_BPL; ++q) {
                     const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
-                    if (merging && lj < N && actq[q] && lj != gq[q]) {
-                        // penetration with the leaf's body (radius kept with
-                        // the entry): a task when the distance is below the
-                        // sum of the radii and this body's index is the smaller
-                        const float rs = my_rad[q] + lrad[j];
-                        if (rx * rx + ry * ry + rz * rz < rs * rs) {
-                            const uint32_t bi = b.idx_in[gq[q]], oi = b.idx_in[lj];
-                            if (bi < oi) {
-                                const uint32_t slot = atomicAdd(&b.mq->tail, 1u);
-                                if (slot < N) {
-                                    b.mq->pairs[slot] = make_uint2(bi, oi);
-                                    b.mkeys[slot] = ((unsigned long long)gq[q] << 32) | seq[q];
-                                }
-                                ++seq[q];
-                            }
-                        }
-                    }
+                    if (merging) merge_test(q, lj, rx, ry, rz, lrad[j]);
                     const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                     const float inv = rsqrtf(rr);
                     const bool self = self_check && lj == gq[q];
@@ -322,6 +341,36 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                 }
             }
         }
+        if (merging && !(PREC || want_pot)) {
+            // merge tests outside the force loop: lane j screens entry j with
+            // the distance from the leaf to the group's box against its radius
+            // plus the group's largest (with a margin for rounding); only the
+            // leaves within reach get the per-body test, in list order
+            const float3 bmn = MODE == GM_LEARNED ? S.geom[w].bmin : gg.bmin;
+            const float3 bmx = MODE == GM_LEARNED ? S.geom[w].bmax : gg.bmax;
+            for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+                bool near = false;
+                if (j0 + lane < cnt && lid[j0 + lane] < N) {
+                    const float4 c = lcm[j0 + lane];
+                    const float dx = fmaxf(fmaxf(bmn.x - c.x, c.x - bmx.x), 0.0f);
+                    const float dy = fmaxf(fmaxf(bmn.y - c.y, c.y - bmx.y), 0.0f);
+                    const float dz = fmaxf(fmaxf(bmn.z - c.z, c.z - bmx.z), 0.0f);
+                    const float reach = lrad[j0 + lane] + S.grp_rad[w];
+                    near = dx * dx + dy * dy + dz * dz <= 1.001f * (reach * reach);
+                }
+                uint32_t m = __ballot_sync(0xffffffffu, near);
+                while (m) {
+                    const uint32_t j = j0 + __ffs(m) - 1;
+                    m &= m - 1;
+                    const float4 c = lcm[j];
+                    const uint32_t lj = lid[j];
+                    const float lr = lrad[j];
+#pragma unroll
+                    for (int q = 0; q < GW_BPL; ++q)
+                        merge_test(q, lj, c.x - pw[q].x, c.y - pw[q].y, c.z - pw[q].z, lr);
+                }
+            }
+        }
         inter += cnt;
     };
     // each lane's outcome: 1 list, 2 open (push children); warp-collective
@@ -341,7 +390,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             else
                 lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
             lid[pos] = id;
-            if (merging) lrad[pos] = id < N ? b.leaf_rad[id] : 0.0f;
+            if (merging) lrad[pos] = lo.x;  // the leaf's radius, read at the pop (0 for nodes)
         }
         ln += __popc(bl);
         if (kind == 2) {
@@ -427,6 +476,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             if (id < N) {
                 cm = b.leaf_pm[id];
                 if (PREC) lo = b.leaf_lo[id];
+                if (merging) lo.x = b.leaf_rad[id];
                 kind = 1;
             } else {
                 const gbh_node* nd = &b.internal[id - N];
