@@ -459,7 +459,10 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     };
 
     while (sp > 0 || np > 0) {
-        if (MODE == GM_LEARNED && sp == 0) {
+        // the network decides the queue before a pop when the stack cannot
+        // fill one and 20 or more rows wait: its opened nodes refill the
+        // stack, so pops run fuller (a decision does not depend on the batch)
+        if (MODE == GM_LEARNED && (sp == 0 || (sp < 32u && np >= 20u))) {
             decide_queue(min(np, 32u));
             continue;
         }
