@@ -72,6 +72,8 @@ def _declare(L):
         "gbh_mac_loss_grad": [vp, vp, vp, u32, C.POINTER(C.c_float), vp],
         "gbh_mac_predict": [vp, vp, u32, vp],
         "gbh_sort_pairs_noalloc": [vp, vp, vp, vp, u32, vp],
+        "gbh_select_glow_nodes": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],
+        "gbh_select_regions": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],
     }
     for name, args in sigs.items():
         f = getattr(L, name)

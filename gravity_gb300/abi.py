@@ -179,6 +179,78 @@ class DeviceBuffers(C.Structure):
     ]
 
 
+class View(C.Structure):
+    """gbh_view: the render uniforms of the node glow and region shaders."""
+    _fields_ = [
+        ("model_view", C.c_float * 16),
+        ("proj", C.c_float * 16),
+        ("fov_y", C.c_float),
+        ("aspect", C.c_float),
+        ("camera_scale", C.c_float),
+        ("relative_to", C.c_uint32),
+        ("glow_theta_ndc", C.c_float),
+        ("glow_activate_dist", C.c_float),
+        ("glow_max_depth", C.c_int32),
+        ("glow_intensity", C.c_float),
+        ("region_min_depth", C.c_int32),
+        ("region_max_depth", C.c_int32),
+        ("pad", C.c_uint32 * 2),
+    ]
+
+
+assert C.sizeof(View) == 176
+
+GLOW_SPLAT_DTYPE = np.dtype([
+    ("center_clip", "<f4", (4,)), ("center_view", "<f4", (3,)), ("intensity", "<f4"), ("color", "<f4", (3,)),
+    ("node", "<u4"), ("ndc_scale", "<f4", (2,)), ("depth", "<u4"), ("pad", "<u4"),
+])
+REGION_DTYPE = np.dtype([("center", "<f4", (3,)), ("size", "<f4", (3,)), ("node", "<u4"), ("depth", "<u4")])
+assert GLOW_SPLAT_DTYPE.itemsize == 64 and REGION_DTYPE.itemsize == 32
+
+
+def view(model_view, proj, fov_y, aspect, camera_scale=10.0, relative_to=0xFFFFFFFF, glow_theta_px=16.0,
+         height=1080, glow_activate_dist=0.0, glow_max_depth=8, glow_intensity=0.003, region_depths=(0, 8)) -> View:
+    """A View from 4x4 matrices (row-major numpy, as written on paper; stored
+    column-major like GLSL) and the reference's Settings defaults
+    (nodeGlowThetaPx 16, nodeGlowActivateDist 0, nodeGlowMaxDepth 8,
+    nodeGlowIntensity 0.003; uNodeGlowThetaNdc = 2 px / height, GPU.java:913-915)."""
+    v = View()
+    mv = np.asarray(model_view, dtype=np.float32).T.reshape(-1)
+    pr = np.asarray(proj, dtype=np.float32).T.reshape(-1)
+    v.model_view[:] = mv.tolist()
+    v.proj[:] = pr.tolist()
+    v.fov_y, v.aspect, v.camera_scale = fov_y, aspect, camera_scale
+    v.relative_to = relative_to
+    v.glow_theta_ndc = np.float32(2.0) * np.float32(glow_theta_px) / np.float32(max(1.0, height))
+    v.glow_activate_dist, v.glow_max_depth, v.glow_intensity = glow_activate_dist, glow_max_depth, glow_intensity
+    v.region_min_depth, v.region_max_depth = region_depths
+    return v
+
+
+def look_at(eye, target, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """Row-major 4x4 view matrix (right-handed, camera looking down -z)."""
+    eye, target, up = (np.asarray(x, dtype=np.float64) for x in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[:3, 3] = -m[:3, :3] @ eye
+    return m.astype(np.float32)
+
+
+def perspective(fov_y, aspect, near, far) -> np.ndarray:
+    """Row-major 4x4 OpenGL perspective projection."""
+    t = 1.0 / np.tan(0.5 * fov_y)
+    m = np.zeros((4, 4))
+    m[0, 0], m[1, 1] = t / aspect, t
+    m[2, 2], m[2, 3] = (far + near) / (near - far), 2 * far * near / (near - far)
+    m[3, 2] = -1.0
+    return m.astype(np.float32)
+
+
 def units(mass=1.0, density=1.0, length=1.0, time=1.0, camera_scale=10.0, G=0.0) -> Units:
     """UnitSet with the reference defaults (defaultProperties.json: 1,1,1,1, cameraScale 10)."""
     return Units(mass, density, length, time, camera_scale, G)

@@ -27,6 +27,7 @@ class BarnesHut:
 
     def __init__(self, initial_num_bodies: int, bounds, units: abi.Units | None = None, device: int = 0):
         self.n = int(initial_num_bodies)
+        self.device = int(device)
         b = np.ascontiguousarray(np.asarray(bounds, dtype=np.float32).reshape(-1))
         if b.size != 6:
             raise ValueError("bounds must hold 6 floats (min xyz, max xyz)")
@@ -279,6 +280,28 @@ class BarnesHut:
         lo, hi = C.c_float(0), C.c_float(0)
         self._chk(lib().gbh_mac_get_band(self._h, C.byref(lo), C.byref(hi)))
         return float(lo.value), float(hi.value)
+
+    # ---- headless node selection (the render shaders' level-of-detail pass) --
+    def _select(self, fn, view: abi.View, dtype: np.dtype, capacity: int | None):
+        """Runs a gbh_select_* entry point into a device buffer (a torch
+        tensor) and copies the records back, sorted by node."""
+        import torch
+
+        cap = max(self.n, 1) if capacity is None else capacity
+        buf = torch.empty((max(cap, 1), dtype.itemsize), dtype=torch.uint8, device=f"cuda:{self.device}")
+        cnt = C.c_uint32(0)
+        self._chk(fn(self._h, C.byref(view), C.c_void_p(buf.data_ptr()), cap, C.byref(cnt)))
+        got = min(cnt.value, cap)
+        out = buf[:got].cpu().numpy().reshape(-1).view(dtype).copy()
+        return np.sort(out, order="node"), cnt.value
+
+    def select_glow_nodes(self, view: abi.View, capacity: int | None = None):
+        """(records, selected): nodeglow.vert's per-node outputs of the drawn nodes."""
+        return self._select(lib().gbh_select_glow_nodes, view, abi.GLOW_SPLAT_DTYPE, capacity)
+
+    def select_regions(self, view: abi.View, capacity: int | None = None):
+        """(records, selected): regions.vert's boxes of the nodes in the depth range."""
+        return self._select(lib().gbh_select_regions, view, abi.REGION_DTYPE, capacity)
 
     def mac_generate(self, params: abi.StepParams, max_pairs: int, seed: int = 0) -> int:
         cnt = C.c_uint32(0)

@@ -63,6 +63,7 @@ struct DevState {
     uint32_t frontier_saturated;       // group walks that accepted instead of opening (full stack)
     uint32_t fill_frontier;            // nodes handed from the tiled fill to the top-tree fill
     uint32_t sorted_valid;             // sorted_pm holds the current positions in index order
+    uint32_t view_count;               // records of the last node selection (gbh_select_*)
     unsigned long long interactions;
     unsigned long long opened;
     unsigned long long mac_evals;

@@ -378,6 +378,64 @@ int gbh_mac_predict(gbh_ctx* ctx, const float* features, uint32_t count, float* 
 int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                            uint32_t* vals_out, uint32_t n, void* stream);
 
+/* ---- headless consumers of the tree: level-of-detail node selection ---------
+ * The reference's render shaders read the internal nodes directly: the
+ * hierarchical node glow (nodeglow.vert:46-150) draws a soft splat at the
+ * centre of mass of every node whose projected size falls inside a band, and
+ * the region boxes (regions.vert:19-45) draw the AABB of every node inside a
+ * depth range.  These entry points run the same per-node arithmetic as CUDA
+ * kernels over the tree of the last step (the bodies of the current state for
+ * `relative_to`) and append one record per selected node to a DEVICE buffer
+ * the caller owns; nothing is drawn.  Records come in no particular order
+ * (sort by `node` for a stable one).  `*count` receives the number of nodes
+ * selected; when it exceeds `capacity`, only `capacity` records are written.
+ * They return after the selection has finished.
+ * Differences from the shaders, both reference defects: only the live internal
+ * nodes [0, n - 1) are visited (the shaders visit every slot up to N - 1 or n,
+ * including stale ones), and tan(fov_y / 2) is computed once on the host. */
+typedef struct gbh_view {
+    float model_view[16];     /* uModelView, column-major (GLSL mat4 memory order) */
+    float proj[16];           /* uProj, column-major */
+    float fov_y;              /* uFovY, radians */
+    float aspect;             /* uAspect */
+    float camera_scale;       /* cameraScale: camera units per length unit */
+    uint32_t relative_to;     /* uRelativeTo: body index, 0xFFFFFFFF = absolute */
+    float glow_theta_ndc;     /* uNodeGlowThetaNdc = 2 * nodeGlowThetaPx / framebuffer height */
+    float glow_activate_dist; /* uNodeGlowActivateDist (view-space depth) */
+    int32_t glow_max_depth;   /* uNodeGlowMaxDepth (node height above its furthest leaf) */
+    float glow_intensity;     /* uNodeGlowIntensity */
+    int32_t region_min_depth; /* uMinMaxDepth.x */
+    int32_t region_max_depth; /* uMinMaxDepth.y */
+    uint32_t pad[2];
+} gbh_view; /* 176 bytes */
+
+/* per selected node: the outputs of nodeglow.vert for its instance (the four
+ * corner vertices add +-1.5 * ndc_scale * center_clip.w to center_clip.xy) */
+typedef struct gbh_glow_splat {
+    float center_clip[4];     /* uProj * uModelView * com */
+    float center_view[3];     /* vCenterView */
+    float intensity;          /* vIntensity (after the Reinhard map) */
+    float color[3];           /* vColor: the node's avgColor.rgb */
+    uint32_t node;            /* internal node index (global id N + node) */
+    float ndc_scale[2];       /* vNdcScaleX, vNdcScaleY */
+    uint32_t depth;           /* nodeDepth */
+    uint32_t pad;
+} gbh_glow_splat; /* 64 bytes */
+
+/* per selected node: the box regions.vert scales its unit cube to (camera
+ * units, relative to `relative_to`), and the depth it passes on */
+typedef struct gbh_region {
+    float center[3];
+    float size[3];
+    uint32_t node;            /* internal node index */
+    uint32_t depth;           /* nodeDepth */
+} gbh_region; /* 32 bytes */
+
+int gbh_select_glow_nodes(gbh_ctx* ctx, const gbh_view* view, gbh_glow_splat* out_device, uint32_t capacity,
+                          uint32_t* count);
+int gbh_select_regions(gbh_ctx* ctx, const gbh_view* view, gbh_region* out_device, uint32_t capacity,
+                       uint32_t* count);
+
 /* ---- library info ---------------------------------------------------------- */
 int gbh_abi_version(void);
 const char* gbh_last_error(gbh_ctx* ctx);

@@ -1029,3 +1029,123 @@ int orc_direct_sum_fp64(const gbh_body* bodies, uint32_t n, const uint32_t* samp
     }
     return GBH_OK;
 }
+
+/* ------------------------------------------------------------------------
+ * Render-side level-of-detail selection (nodeglow.vert:46-150,
+ * regions.vert:19-45), restated in FP32 with one rounding per operation.
+ * mat4 * vec4 follows GLSL's column-major layout, columns added in order.
+ * ------------------------------------------------------------------------ */
+static void view_rel(const float a[3], const gbh_view* v, const gbh_body* bodies, uint32_t cap, float out[3]) {
+    /* relativeLocation, common.glsl:291-299 */
+    if (v->relative_to == 0xFFFFFFFFu || v->relative_to >= cap) {
+        out[0] = a[0];
+        out[1] = a[1];
+        out[2] = a[2];
+        return;
+    }
+    const float* p = bodies[v->relative_to].pos_mass;
+    out[0] = a[0] - p[0];
+    out[1] = a[1] - p[1];
+    out[2] = a[2] - p[2];
+}
+
+static void view_mat4(const float m[16], const float x[4], float r[4]) {
+    for (int row = 0; row < 4; ++row)
+        r[row] = m[row] * x[0] + m[4 + row] * x[1] + m[8 + row] * x[2] + m[12 + row] * x[3];
+}
+
+static float view_smoothstep(float e0, float e1, float x) {
+    /* GLSL smoothstep: t = clamp((x - e0) / (e1 - e0), 0, 1), t^2 (3 - 2t) */
+    float t = (x - e0) / (e1 - e0);
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+/* the AABB corners relative to view->relative_to, times cameraScale */
+static void view_box(const gbh_node* nd, const gbh_view* v, const gbh_body* bodies, uint32_t cap, float mn[3],
+                     float mx[3]) {
+    float a[3], b[3];
+    view_rel(&nd->aabb[0], v, bodies, cap, a);
+    view_rel(&nd->aabb[3], v, bodies, cap, b);
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = a[k] * v->camera_scale;
+        mx[k] = b[k] * v->camera_scale;
+    }
+}
+
+uint32_t orc_select_glow_nodes(const gbh_node* internal, uint32_t count, const gbh_body* bodies,
+                               uint32_t num_bodies_cap, const gbh_view* v, gbh_glow_splat* out, uint32_t capacity) {
+    const float tan_half = tanf(0.5f * v->fov_y);
+    uint32_t sel = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbh_node* nd = &internal[i];
+        /* culls in the shader's order */
+        if (nd->aabb[0] > nd->aabb[3] || nd->com_mass[3] <= 0.0f || nd->bodies_contained == 0u) continue;
+        if (nd->node_depth < 1u || nd->node_depth > (uint32_t)v->glow_max_depth) continue;
+        float mn[3], mx[3];
+        view_box(nd, v, bodies, num_bodies_cap, mn, mx);
+        const float sx = mx[0] - mn[0], sy = mx[1] - mn[1], sz = mx[2] - mn[2];
+        const float longest = fmaxf(sx, fmaxf(sy, sz));
+        const float half_extent = 0.5f * longest;
+        float com[3];
+        view_rel(nd->com_mass, v, bodies, num_bodies_cap, com);
+        const float com4[4] = {com[0] * v->camera_scale, com[1] * v->camera_scale, com[2] * v->camera_scale, 1.0f};
+        float cv[4];
+        view_mat4(v->model_view, com4, cv);
+        const float cam_dist = fmaxf(-cv[2], 1e-6f);
+        if (cam_dist < v->glow_activate_dist) continue;
+        const float projected = longest / (cam_dist * tan_half);
+        const float theta_ndc = fmaxf(v->glow_theta_ndc, 1e-6f);
+        const float min_ndc = theta_ndc * 0.04f;
+        if (projected >= theta_ndc || projected < min_ndc) continue;
+        float accept = 1.0f - view_smoothstep(theta_ndc * 0.75f, theta_ndc, projected);
+        accept = accept * view_smoothstep(min_ndc, min_ndc * 2.5f, projected);
+        const float area = fmaxf(projected * projected, 1e-8f);
+        const float luminosity = nd->com_mass[3] * (1.0e6f / (cam_dist * cam_dist));
+        const float surface = luminosity / area;
+        const float raw = surface * 2.5e-4f * accept * v->glow_intensity;
+        const float intensity = raw / (1.0f + raw);
+        if (intensity < 1e-4f) continue;
+        if (sel < capacity) {
+            gbh_glow_splat* r = &out[sel];
+            float clip[4];
+            view_mat4(v->proj, cv, clip);
+            const float glow_half = fmaxf(half_extent * 1.1f, min_ndc * 0.5f * cam_dist * tan_half);
+            const float ndc_y = glow_half / (cam_dist * tan_half);
+            memcpy(r->center_clip, clip, sizeof(clip));
+            memcpy(r->center_view, cv, 3 * sizeof(float));
+            r->intensity = intensity;
+            memcpy(r->color, nd->avg_color, 3 * sizeof(float));
+            r->node = i;
+            r->ndc_scale[0] = ndc_y / fmaxf(v->aspect, 1e-6f);
+            r->ndc_scale[1] = ndc_y;
+            r->depth = nd->node_depth;
+            r->pad = 0;
+        }
+        ++sel;
+    }
+    return sel;
+}
+
+uint32_t orc_select_regions(const gbh_node* internal, uint32_t count, const gbh_body* bodies,
+                            uint32_t num_bodies_cap, const gbh_view* v, gbh_region* out, uint32_t capacity) {
+    uint32_t sel = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbh_node* nd = &internal[i];
+        if (nd->aabb[0] > nd->aabb[3]) continue;
+        if (nd->node_depth < (uint32_t)v->region_min_depth || nd->node_depth > (uint32_t)v->region_max_depth) continue;
+        if (sel < capacity) {
+            float mn[3], mx[3];
+            view_box(nd, v, bodies, num_bodies_cap, mn, mx);
+            gbh_region* r = &out[sel];
+            for (int k = 0; k < 3; ++k) {
+                r->center[k] = (mn[k] + mx[k]) * 0.5f;
+                r->size[k] = mx[k] - mn[k];
+            }
+            r->node = i;
+            r->depth = nd->node_depth;
+        }
+        ++sel;
+    }
+    return sel;
+}

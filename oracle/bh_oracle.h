@@ -81,6 +81,18 @@ uint64_t orc_morton_encode(const float pos[3], const float bmin[3], const float 
 int orc_safe_lcp(const uint64_t* keys, int n, int i, int j);
 void orc_star_color(float mass, float density, float rgb[3]);
 
+/* Level-of-detail node selection of the render shaders, restated: the
+ * hierarchical node glow (nodeglow.vert:46-150) and the region boxes
+ * (regions.vert:19-45) over internal[0..count), the live internal nodes.
+ * `bodies` is the state's body buffer (for view->relative_to) and
+ * `num_bodies_cap` its length (initial_num_bodies).  Records are written in
+ * node order, at most `capacity`; the return value is the number selected. */
+uint32_t orc_select_glow_nodes(const gbh_node* internal, uint32_t count, const gbh_body* bodies,
+                               uint32_t num_bodies_cap, const gbh_view* view, gbh_glow_splat* out,
+                               uint32_t capacity);
+uint32_t orc_select_regions(const gbh_node* internal, uint32_t count, const gbh_body* bodies,
+                            uint32_t num_bodies_cap, const gbh_view* view, gbh_region* out, uint32_t capacity);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,10 @@ def lib():
         L.orc_morton_encode.argtypes = [C.POINTER(C.c_float)] * 3
         L.orc_star_color.restype = None
         L.orc_star_color.argtypes = [C.c_float, C.c_float, C.POINTER(C.c_float)]
+        for name in ("orc_select_glow_nodes", "orc_select_regions"):
+            f = getattr(L, name)
+            f.restype = u32
+            f.argtypes = [vp, u32, vp, u32, C.POINTER(abi.View), vp, u32]
         _lib = L
     return _lib
 
@@ -260,6 +264,24 @@ def direct_sum_fp64(bodies: np.ndarray, sample: np.ndarray, G: float, softening:
     out = np.zeros((len(s), 3), dtype=np.float64)
     _check(lib().orc_direct_sum_fp64(_ptr(b), len(b), _ptr(s), len(s), G, softening, _ptr(out)), "direct_sum")
     return out
+
+
+def _select(fn, internal: np.ndarray, bodies: np.ndarray, view: abi.View, dtype: np.dtype):
+    nodes = np.ascontiguousarray(internal, dtype=abi.NODE_DTYPE)
+    b = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+    out = np.zeros(max(len(nodes), 1), dtype=dtype)
+    sel = fn(_ptr(nodes), len(nodes), _ptr(b), len(b), C.byref(view), _ptr(out), len(out))
+    return out[:min(sel, len(out))], int(sel)
+
+
+def select_glow_nodes(internal: np.ndarray, bodies: np.ndarray, view: abi.View):
+    """(records in node order, selected) of nodeglow.vert over the live internal nodes."""
+    return _select(lib().orc_select_glow_nodes, internal, bodies, view, abi.GLOW_SPLAT_DTYPE)
+
+
+def select_regions(internal: np.ndarray, bodies: np.ndarray, view: abi.View):
+    """(records in node order, selected) of regions.vert over the live internal nodes."""
+    return _select(lib().orc_select_regions, internal, bodies, view, abi.REGION_DTYPE)
 
 
 def morton_encode(pos, bmin, bmax) -> int:

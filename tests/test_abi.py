@@ -64,6 +64,11 @@ int main(void) {
   P(gbh_sim_values, gravitational_constant); P(gbh_sim_values, uint_debug); P(gbh_sim_values, float_debug);
   P(gbh_step_params, units); P(gbh_step_params, mac_mode); P(gbh_step_params, flags);
   P(gbh_stats, alive); P(gbh_stats, error_word);
+  printf("sizeof.gbh_view %zu\nsizeof.gbh_glow_splat %zu\nsizeof.gbh_region %zu\n", sizeof(gbh_view),
+         sizeof(gbh_glow_splat), sizeof(gbh_region));
+  P(gbh_view, fov_y); P(gbh_view, relative_to); P(gbh_view, glow_intensity); P(gbh_view, region_max_depth);
+  P(gbh_glow_splat, intensity); P(gbh_glow_splat, node); P(gbh_glow_splat, ndc_scale); P(gbh_glow_splat, depth);
+  P(gbh_region, node); P(gbh_region, depth);
   return 0;
 }
 """
@@ -96,6 +101,15 @@ def test_struct_layouts_match_header():
     assert got["gbh_step_params.flags"] == abi.StepParams.flags.offset
     assert got["gbh_stats.alive"] == abi.Stats.alive.offset
     assert got["gbh_stats.error_word"] == abi.Stats.error_word.offset
+    assert got["sizeof.gbh_view"] == C.sizeof(abi.View) == 176
+    for f in ("fov_y", "relative_to", "glow_intensity", "region_max_depth"):
+        assert got[f"gbh_view.{f}"] == getattr(abi.View, f).offset
+    assert got["sizeof.gbh_glow_splat"] == abi.GLOW_SPLAT_DTYPE.itemsize
+    for f in ("intensity", "node", "ndc_scale", "depth"):
+        assert got[f"gbh_glow_splat.{f}"] == abi.GLOW_SPLAT_DTYPE.fields[f][1]
+    assert got["sizeof.gbh_region"] == abi.REGION_DTYPE.itemsize
+    for f in ("node", "depth"):
+        assert got[f"gbh_region.{f}"] == abi.REGION_DTYPE.fields[f][1]
 
 
 def test_body_layout_is_two_vec4():
