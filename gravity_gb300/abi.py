@@ -179,6 +179,55 @@ class DeviceBuffers(C.Structure):
     ]
 
 
+IC_BOX, IC_DISK, IC_PLUMMER, IC_CLUSTERS = 0, 1, 2, 3
+IC_ORBITAL, IC_CCW = 0x1, 0x2
+
+
+class IcParams(C.Structure):
+    """gbh_ic_params: seeded initial conditions generated on the device."""
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("flags", C.c_uint32),
+        ("lo", C.c_float * 8),
+        ("hi", C.c_float * 8),
+        ("center", C.c_float * 3),
+        ("velocity", C.c_float * 3),
+        ("scale", C.c_float),
+        ("total_mass", C.c_float),
+        ("density", C.c_float),
+        ("G", C.c_float),
+        ("phi", C.c_float),
+        ("center_mass", C.c_float),
+        ("center_density", C.c_float),
+        ("adherence", C.c_float),
+        ("orbital_factor", C.c_float),
+        ("clusters", C.c_uint32),
+        ("sigma_lo", C.c_float),
+        ("sigma_hi", C.c_float),
+    ]
+
+
+assert C.sizeof(IcParams) == 144
+
+
+def ic_params(kind, **kw) -> IcParams:
+    """IcParams of `kind` with fields from keywords; `ranges` = 8 (lo, hi)
+    pairs for x, y, z, vx, vy, vz, mass, density."""
+    p = IcParams()
+    p.kind = kind
+    p.density, p.G, p.scale, p.total_mass = 1.0, 1.0, 1.0, 1.0
+    ranges = kw.pop("ranges", None)
+    if ranges is not None:
+        for k, (lo, hi) in enumerate(ranges):
+            p.lo[k], p.hi[k] = lo, hi
+    for name, val in kw.items():
+        if name in ("center", "velocity"):
+            getattr(p, name)[:] = list(val)
+        else:
+            setattr(p, name, val)
+    return p
+
+
 class View(C.Structure):
     """gbh_view: the render uniforms of the node glow and region shaders."""
     _fields_ = [

@@ -70,6 +70,11 @@ class BarnesHut:
             part = b[s : s + chunk]
             self._chk(lib().gbh_upload_bodies(self._h, _ptr(part), len(part), offset + s))
 
+    def generate_bodies(self, params: abi.IcParams, seed: int = 0, count: int | None = None, offset: int = 0):
+        """Seeded initial conditions written on the device (gbh_generate_bodies)."""
+        count = self.n - offset if count is None else count
+        self._chk(lib().gbh_generate_bodies(self._h, C.byref(params), seed, count, offset))
+
     def init(self):
         self._chk(lib().gbh_init(self._h))
 

@@ -301,6 +301,8 @@ __device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
 void launch_reset(const StepBuffers& b, cudaStream_t s);
 void launch_prepare(const StepBuffers& b, cudaStream_t s);
 void launch_sort(const StepBuffers& b, cudaStream_t s);
+void launch_generate_bodies(gbh_body* bodies, uint32_t count, uint32_t offset, const gbh_ic_params& p, uint64_t seed,
+                            cudaStream_t s);
 void launch_build(const StepBuffers& b, cudaStream_t s);
 void launch_fill(const StepBuffers& b, cudaStream_t s);
 void launch_build_nodes(const StepBuffers& b, cudaStream_t s);

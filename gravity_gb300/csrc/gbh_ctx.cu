@@ -389,6 +389,25 @@ int gbh_upload_bodies(gbh_ctx* c, const gbh_body* host, uint32_t count, uint32_t
     return GBH_OK;
 }
 
+int gbh_generate_bodies(gbh_ctx* c, const gbh_ic_params* p, uint64_t seed, uint32_t count, uint32_t offset) {
+    if (!c || !p) return fail(c, GBH_ERR_INVALID, "null argument");
+    if ((uint64_t)offset + count > c->N) return fail(c, GBH_ERR_INVALID, "generate range exceeds initial_num_bodies");
+    if (p->kind > GBH_IC_CLUSTERS) return fail(c, GBH_ERR_INVALID, "unknown initial-condition kind");
+    if (p->kind == GBH_IC_CLUSTERS && !(p->sigma_lo > 0.0f && p->sigma_hi > 0.0f && p->lo[6] > 0.0f && p->hi[6] > 0.0f))
+        return fail(c, GBH_ERR_INVALID, "cluster sigmas and masses must be positive");
+    if (p->kind == GBH_IC_PLUMMER && !(p->scale > 0.0f)) return fail(c, GBH_ERR_INVALID, "Plummer scale must be positive");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_generate_bodies(c->bodies[c->bin], count, offset, *p, seed, c->stream);
+    CUDA_TRY(c, cudaGetLastError());
+    // the same bookkeeping as an upload
+    c->pos64_valid = false;
+    ++c->state_epoch;
+    int rc = invalidate_sorted(c);
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
 int gbh_init(gbh_ctx* c) {
     if (!c) return fail(c, GBH_ERR_INVALID, "null context");
     CUDA_TRY(c, cudaSetDevice(c->device));

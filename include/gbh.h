@@ -378,6 +378,59 @@ int gbh_mac_predict(gbh_ctx* ctx, const float* features, uint32_t count, float* 
 int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                            uint32_t* vals_out, uint32_t n, void* stream);
 
+/* ---- seeded initial conditions, generated on the device ----------------------
+ * gbh_generate_bodies writes bodies [offset, offset + count) of the current
+ * body buffer (like gbh_upload_bodies, without a host copy).  Every number is
+ * drawn from a counter-based generator keyed by (seed, body index, draw), so
+ * a range generated in chunks equals the same range generated at once, on any
+ * GPU.  Kinds:
+ *   GBH_IC_BOX       makeNewRandomBox (PlanetGenerator.java:310-321): x, y, z,
+ *                    vx, vy, vz, mass, density each uniform in [lo[k], hi[k]].
+ *   GBH_IC_DISK      makeNewRandomDisk (PlanetGenerator.java:418-489): count - 1
+ *                    disk bodies and, last, the centre body.  Radius uniform in
+ *                    [lo[0], hi[0]], mass in [lo[6], hi[6]], density in
+ *                    [lo[7], hi[7]]; disk normal (0, sin phi, cos phi); the
+ *                    deviation from the plane pi (1 - U^(1 - adherence)) above
+ *                    or below it; orbital speed sqrt((centre_mass + approximate
+ *                    enclosed mass) G / r) * orbital_factor when flags has
+ *                    GBH_IC_ORBITAL, counter-clockwise with GBH_IC_CCW.
+ *   GBH_IC_PLUMMER   Plummer sphere of scale radius `scale` and mass
+ *                    `total_mass` in `count` equal bodies (the count of this
+ *                    call; chunks keep positions and velocities) (Aarseth, Henon & Wielen 1974:
+ *                    radius from the mass fraction, speed by rejection from
+ *                    q^2 (1 - q^2)^(7/2), isotropic directions), density `density`.
+ *   GBH_IC_CLUSTERS  `clusters` isotropic Gaussians: centres uniform in
+ *                    [-scale, scale]^3, sigma log-uniform in [sigma_lo, sigma_hi],
+ *                    each body in a uniformly chosen cluster; masses from the
+ *                    power law dN/dm ~ m^-2 on [lo[6], hi[6]]; density `density`.
+ * DISK and PLUMMER add `center` and `velocity` to every body. */
+#define GBH_IC_BOX 0u
+#define GBH_IC_DISK 1u
+#define GBH_IC_PLUMMER 2u
+#define GBH_IC_CLUSTERS 3u
+#define GBH_IC_ORBITAL 0x1u
+#define GBH_IC_CCW 0x2u
+typedef struct gbh_ic_params {
+    uint32_t kind;           /* GBH_IC_* */
+    uint32_t flags;          /* DISK: GBH_IC_ORBITAL | GBH_IC_CCW */
+    float lo[8];             /* ranges: x, y, z, vx, vy, vz, mass, density (see the kinds) */
+    float hi[8];
+    float center[3];
+    float velocity[3];
+    float scale;             /* PLUMMER: scale radius; CLUSTERS: half side of the centres' cube */
+    float total_mass;        /* PLUMMER */
+    float density;           /* PLUMMER, CLUSTERS */
+    float G;                 /* PLUMMER, DISK: gravitational constant of the velocities */
+    float phi;               /* DISK: tilt of the normal about x */
+    float center_mass;       /* DISK */
+    float center_density;    /* DISK (also the exponent of the enclosed-mass estimate, as the reference) */
+    float adherence;         /* DISK: adherenceToPlane */
+    float orbital_factor;    /* DISK */
+    uint32_t clusters;       /* CLUSTERS */
+    float sigma_lo, sigma_hi;/* CLUSTERS */
+} gbh_ic_params; /* 144 bytes */
+int gbh_generate_bodies(gbh_ctx* ctx, const gbh_ic_params* params, uint64_t seed, uint32_t count, uint32_t offset);
+
 /* ---- headless consumers of the tree: level-of-detail node selection ---------
  * The reference's render shaders read the internal nodes directly: the
  * hierarchical node glow (nodeglow.vert:46-150) draws a soft splat at the

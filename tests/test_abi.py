@@ -69,6 +69,8 @@ int main(void) {
   P(gbh_view, fov_y); P(gbh_view, relative_to); P(gbh_view, glow_intensity); P(gbh_view, region_max_depth);
   P(gbh_glow_splat, intensity); P(gbh_glow_splat, node); P(gbh_glow_splat, ndc_scale); P(gbh_glow_splat, depth);
   P(gbh_region, node); P(gbh_region, depth);
+  printf("sizeof.gbh_ic_params %zu\n", sizeof(gbh_ic_params));
+  P(gbh_ic_params, center); P(gbh_ic_params, G); P(gbh_ic_params, clusters); P(gbh_ic_params, sigma_hi);
   return 0;
 }
 """
@@ -107,6 +109,9 @@ def test_struct_layouts_match_header():
     assert got["sizeof.gbh_glow_splat"] == abi.GLOW_SPLAT_DTYPE.itemsize
     for f in ("intensity", "node", "ndc_scale", "depth"):
         assert got[f"gbh_glow_splat.{f}"] == abi.GLOW_SPLAT_DTYPE.fields[f][1]
+    assert got["sizeof.gbh_ic_params"] == C.sizeof(abi.IcParams) == 144
+    for f in ("center", "G", "clusters", "sigma_hi"):
+        assert got[f"gbh_ic_params.{f}"] == getattr(abi.IcParams, f).offset
     assert got["sizeof.gbh_region"] == abi.REGION_DTYPE.itemsize
     for f in ("node", "depth"):
         assert got[f"gbh_region.{f}"] == abi.REGION_DTYPE.fields[f][1]
