@@ -25,6 +25,7 @@
 // the MLP's training data (gbh_mac_generate).
 // Only gravity (merging_collision_or_neither == 0) runs here.
 #include <cstddef>
+#include <type_traits>
 
 #include "gbh_ctx.h"
 #include "mac_mlp.cuh"
@@ -280,6 +281,9 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         }
     };
     auto flush = [&](uint32_t cnt) {
+        // body slots in use: slot q holds bodies 32 q .. 32 q + 31 of the
+        // group, so slots at or above nq are empty in every lane
+        const int nq = (int)((grp.y + 31u) >> 5);
         if (PREC || want_pot) {
             // the general loop: leaf terms apart (PREC), potential, self
             // check, merge tasks
@@ -326,20 +330,31 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                 }
             }
         } else {
+            // one loop per number of slots in use (warp-uniform), unrolled
+            // over a constant
+            auto slots = [&](auto qn) {
+                constexpr int Q = decltype(qn)::value;
 #pragma unroll 2
-            for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 c = lcm[j];
+                for (uint32_t j = 0; j < cnt; ++j) {
+                    const float4 c = lcm[j];
 #pragma unroll
-                for (int q = 0; q < GW_BPL; ++q) {
-                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
-                    const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-                    const float inv = rsqrtf(rr);
-                    const float f = c.w * (inv * inv * inv);
-                    ax[q] = __fmaf_rn(f, rx, ax[q]);
-                    ay[q] = __fmaf_rn(f, ry, ay[q]);
-                    az[q] = __fmaf_rn(f, rz, az[q]);
+                    for (int q = 0; q < Q; ++q) {
+                        const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                        const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                        const float inv = rsqrtf(rr);
+                        const float f = c.w * (inv * inv * inv);
+                        ax[q] = __fmaf_rn(f, rx, ax[q]);
+                        ay[q] = __fmaf_rn(f, ry, ay[q]);
+                        az[q] = __fmaf_rn(f, rz, az[q]);
+                    }
                 }
-            }
+            };
+            if (nq >= GW_BPL)
+                slots(std::integral_constant<int, GW_BPL>{});
+            else if (nq == 2)
+                slots(std::integral_constant<int, 2>{});
+            else
+                slots(std::integral_constant<int, 1>{});
         }
         if (merging && !(PREC || want_pot)) {
             // merge tests outside the force loop: lane j screens entry j with
