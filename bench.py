@@ -312,7 +312,7 @@ PLAIN_THETAS = [0.3, 0.5, 0.7]
 # dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture
 # (profiles/walk_learned_mixture4M.md), divided by its bodies; the walk's
 # traffic grows in proportion to the bodies
-WALK_LEARNED_DRAM_BYTES_PER_BODY = 298.0  # learned walk DRAM read + write per body, 4M ncu capture
+WALK_LEARNED_DRAM_BYTES_PER_BODY = 301.0  # learned walk DRAM read + write per body, 4M ncu capture
 
 
 def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
