@@ -72,6 +72,7 @@ def _declare(L):
         "gbh_mac_loss_grad": [vp, vp, vp, u32, C.POINTER(C.c_float), vp],
         "gbh_mac_predict": [vp, vp, u32, vp],
         "gbh_sort_pairs_noalloc": [vp, vp, vp, vp, u32, vp],
+        "gbh_exchange_bodies": [vp, vp, vp, u32, u32],
         "gbh_generate_bodies": [vp, C.POINTER(abi.IcParams), u64, u32, u32],
         "gbh_select_glow_nodes": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],
         "gbh_select_regions": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],

@@ -70,6 +70,15 @@ class BarnesHut:
             part = b[s : s + chunk]
             self._chk(lib().gbh_upload_bodies(self._h, _ptr(part), len(part), offset + s))
 
+    def exchange_bodies(self, out: np.ndarray, bodies: np.ndarray, offset: int = 0):
+        """Read the current bodies into `out` and install `bodies` in their
+        place, the two copies overlapped (gbh_exchange_bodies)."""
+        b = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+        if out.dtype != abi.BODY_DTYPE or len(out) < len(b) or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous BODY_DTYPE array of at least len(bodies) bodies")
+        self._chk(lib().gbh_exchange_bodies(self._h, _ptr(out), _ptr(b), len(b), offset))
+        return out
+
     def generate_bodies(self, params: abi.IcParams, seed: int = 0, count: int | None = None, offset: int = 0):
         """Seeded initial conditions written on the device (gbh_generate_bodies)."""
         count = self.n - offset if count is None else count

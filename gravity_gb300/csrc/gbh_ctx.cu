@@ -370,6 +370,12 @@ int gbh_destroy(gbh_ctx* c) {
     cudaFree(c->leaf_lo);
     cudaFree(c->potential);
     if (c->arena) cudaFree(c->arena);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        for (cudaEvent_t& e : c->copy_events)
+            if (e) cudaEventDestroy(e);
+        cudaStreamDestroy(c->copy_stream);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return GBH_OK;
@@ -385,6 +391,39 @@ int gbh_upload_bodies(gbh_ctx* c, const gbh_body* host, uint32_t count, uint32_t
     ++c->state_epoch;
     int rc = invalidate_sorted(c);
     if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_exchange_bodies(gbh_ctx* c, gbh_body* host_out, const gbh_body* host_in, uint32_t count, uint32_t offset) {
+    if (!c || !host_out || !host_in) return fail(c, GBH_ERR_INVALID, "null argument");
+    if ((uint64_t)offset + count > c->N) return fail(c, GBH_ERR_INVALID, "exchange range exceeds initial_num_bodies");
+    if (!count) return GBH_OK;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    constexpr uint32_t CHUNKS = sizeof(c->copy_events) / sizeof(c->copy_events[0]);
+    if (!c->copy_stream) {
+        CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : c->copy_events) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    gbh_body* dev = c->bodies[c->bin] + offset;
+    // the read-back starts once the work queued so far (the last step) is done
+    CUDA_TRY(c, cudaEventRecord(c->copy_events[0], c->stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->copy_events[0], 0));
+    const uint32_t per = (count + CHUNKS - 1) / CHUNKS;
+    for (uint32_t k = 0, s = 0; s < count; ++k, s += per) {
+        const size_t bytes = (size_t)min(per, count - s) * sizeof(gbh_body);
+        // chunk k out on the copy stream, then in on the context stream:
+        // the two directions overlap chunk by chunk
+        CUDA_TRY(c, cudaMemcpyAsync(host_out + s, dev + s, bytes, cudaMemcpyDeviceToHost, c->copy_stream));
+        CUDA_TRY(c, cudaEventRecord(c->copy_events[k], c->copy_stream));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->copy_events[k], 0));
+        CUDA_TRY(c, cudaMemcpyAsync(dev + s, host_in + s, bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    c->pos64_valid = false;
+    ++c->state_epoch;
+    int rc = invalidate_sorted(c);
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return GBH_OK;
 }

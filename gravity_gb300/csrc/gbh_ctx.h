@@ -69,6 +69,11 @@ struct gbh_ctx {
     bool mac_ready = false;
     MacState* mac = nullptr;
 
+    // gbh_exchange_bodies: a second stream for the device-to-host half and
+    // one event per chunk (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_events[16] = {};
+
     std::map<int, cudaGraphExec_t> graphs;
     std::string last_error;
 };

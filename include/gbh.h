@@ -209,6 +209,14 @@ int gbh_destroy(gbh_ctx* ctx);
 /* GPU.uploadPlanetsData (GPU.java:1166-1196): copy `count` bodies into the
  * current body buffer starting at body `offset` (chunked uploads allowed). */
 int gbh_upload_bodies(gbh_ctx* ctx, const gbh_body* host, uint32_t count, uint32_t offset);
+/* Read bodies [offset, offset + count) of the current body buffer into
+ * `host_out` and replace them with `host_in`, in one call: the range moves in
+ * chunks, each chunk's upload waiting only for its own read-back, so the two
+ * directions run at the same time on the GPU's two copy engines (with pinned
+ * host memory).  For a host that streams states through the simulation: one
+ * call per step returns the last step's bodies and installs the next input.
+ * Returns when both copies have finished; the buffers must not overlap. */
+int gbh_exchange_bodies(gbh_ctx* ctx, gbh_body* host_out, const gbh_body* host_in, uint32_t count, uint32_t offset);
 
 /* BarnesHut.init (BarnesHut.java:170-173, bh_init.comp:10-27): identity index,
  * derive G and the body length constant. */
