@@ -98,6 +98,7 @@ struct StepBuffers {
     const gbh_step_params* params;
     MergeQueue* mq;
     unsigned long long* mkeys;  // merge ordering keys (slot << 32 | seq)
+    uint32_t* mslots;           // per merge task: the sorted slot of its second body
     uint32_t* locks;
     uint32_t* conflicts;
     float4* accel;

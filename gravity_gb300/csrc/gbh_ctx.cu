@@ -70,6 +70,7 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.params = c->params_dev;
     b.mq = c->mq;
     b.mkeys = c->mkeys;
+    b.mslots = c->mslots;
     b.locks = c->locks;
     b.conflicts = c->conflicts;
     b.accel = c->accel;
@@ -276,7 +277,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_lpm = A.add((size_t)n * 16), o_lrad = A.add((size_t)n * 4), o_spm = A.add((size_t)n * 16);
     size_t o_sim = A.add(sizeof(gbh_sim_values)), o_st = A.add(sizeof(DevState));
     size_t o_par = A.add(sizeof(gbh_step_params));
-    size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8);
+    size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8), o_mslots = A.add((size_t)n * 4);
     size_t o_locks = A.add((size_t)n * 4), o_conf = A.add((size_t)n * 4);
     size_t o_accel = A.add((size_t)n * 16), o_amag = A.add((size_t)n * 4);
     size_t o_nlo = A.add((size_t)ni * 4), o_groups = A.add((size_t)n * 8);
@@ -311,6 +312,7 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->params_dev = (gbh_step_params*)(base + o_par);
     c->mq = (MergeQueue*)(base + o_mq);
     c->mkeys = (unsigned long long*)(base + o_mkeys);
+    c->mslots = (uint32_t*)(base + o_mslots);
     c->locks = (uint32_t*)(base + o_locks);
     c->conflicts = (uint32_t*)(base + o_conf);
     c->accel = (float4*)(base + o_accel);

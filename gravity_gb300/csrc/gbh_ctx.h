@@ -37,6 +37,7 @@ struct gbh_ctx {
     gbh_step_params* params_dev = nullptr;
     MergeQueue* mq = nullptr;
     unsigned long long* mkeys = nullptr;
+    uint32_t* mslots = nullptr;
     uint32_t* locks = nullptr;
     uint32_t* conflicts = nullptr;
     float4* accel = nullptr;

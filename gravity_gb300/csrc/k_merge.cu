@@ -46,9 +46,12 @@ __device__ __forceinline__ void merge_two(float4& p1, float4& v1, const float4 p
     v1 = nv;
 }
 
-// apply task (a, b) on the output bodies; returns true when merged
-__device__ __forceinline__ bool apply_task(gbh_body* dst, uint32_t a, uint32_t c) {
+// apply task t, bodies (a, c), on the output bodies, and keep the in-order
+// copy of the positions (sorted slots of a and c) equal to them; returns true
+// when merged
+__device__ __forceinline__ bool apply_task(const StepBuffers& b, uint32_t t, uint32_t a, uint32_t c) {
     if (a == c) return false;
+    gbh_body* dst = b.bodies_out;
     float4 p1 = ld_pos_mass(dst, a), v1 = ld_vel_density(dst, a);
     const float4 p2 = ld_pos_mass(dst, c), v2 = ld_vel_density(dst, c);
     if (p1.w == 0.0f || p2.w == 0.0f) return false;
@@ -56,6 +59,8 @@ __device__ __forceinline__ bool apply_task(gbh_body* dst, uint32_t a, uint32_t c
     st_body(dst, a, p1, v1);
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     st_body(dst, c, z, z);
+    b.sorted_pm[(uint32_t)(b.mkeys[t] >> 32)] = p1;
+    b.sorted_pm[b.mslots[t]] = z;
     return true;
 }
 
@@ -74,7 +79,7 @@ __global__ void k_merge_apply(StepBuffers b) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
         const uint2 pr = b.mq->pairs[t];
         if (b.locks[pr.x] == 1u && b.locks[pr.y] == 1u) {
-            merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+            merged += apply_task(b, t, pr.x, pr.y) ? 1u : 0u;
         } else {
             const uint32_t slot = atomicAdd(&b.st->merge_conflicts, 1u);
             b.conflicts[slot] = t;
@@ -96,8 +101,9 @@ __global__ __launch_bounds__(MERGE_SORT_THREADS) void k_merge_conflicts(StepBuff
             set_error(b.st, GBH_DEVERR_MERGE_OVERFLOW);
             uint32_t merged = 0;
             for (uint32_t k = 0; k < C; ++k) {
-                const uint2 pr = b.mq->pairs[b.conflicts[k]];
-                merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+                const uint32_t t = b.conflicts[k];
+                const uint2 pr = b.mq->pairs[t];
+                merged += apply_task(b, t, pr.x, pr.y) ? 1u : 0u;
             }
             b.st->merged += merged;
         }
@@ -139,16 +145,15 @@ __global__ __launch_bounds__(MERGE_SORT_THREADS) void k_merge_conflicts(StepBuff
     if (threadIdx.x == 0) {
         uint32_t merged = 0;
         for (uint32_t k = 0; k < C; ++k) {
-            const uint2 pr = b.mq->pairs[s_task[k]];
-            merged += apply_task(b.bodies_out, pr.x, pr.y) ? 1u : 0u;
+            const uint32_t t = s_task[k];
+            const uint2 pr = b.mq->pairs[t];
+            merged += apply_task(b, t, pr.x, pr.y) ? 1u : 0u;
         }
         b.st->merged += merged;
     }
 }
 
 __global__ void k_merge_clear(StepBuffers b) {
-    // merged bodies changed after the walk wrote sorted_pm: the next step gathers
-    if (blockIdx.x == 0 && threadIdx.x == 0 && b.st->merged) b.st->sorted_valid = 0u;
     const uint32_t M = min(b.mq->tail, b.N);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
         const uint2 pr = b.mq->pairs[t];

@@ -150,6 +150,7 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
                     if (slot < N) {
                         b.mq->pairs[slot] = make_uint2(bi, oi);
                         b.mkeys[slot] = ((unsigned long long)g << 32) | seq;
+                        b.mslots[slot] = cur_id;
                     }
                     ++seq;
                 }

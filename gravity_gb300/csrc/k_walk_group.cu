@@ -274,6 +274,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                     if (slot < N) {
                         b.mq->pairs[slot] = make_uint2(bi, oi);
                         b.mkeys[slot] = ((unsigned long long)gq[q] << 32) | seq[q * 32 + lane];
+                        b.mslots[slot] = lj;
                     }
                     ++seq[q * 32 + lane];
                 }
