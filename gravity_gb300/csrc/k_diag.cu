@@ -93,7 +93,10 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __res
                                                              const uint32_t* __restrict__ sample, uint32_t count,
                                                              double G, double soft, uint32_t chunks,
                                                              double* __restrict__ partial) {
-    __shared__ double4 s_src[DS_TILE / 2];
+    struct Src {
+        double x, y, z, w;  // FP64 position and mass of a source body
+    };
+    __shared__ Src s_src[DS_TILE / 2];
     const uint32_t t = blockIdx.x * DS_THREADS + threadIdx.x;
     const uint32_t chunk = blockIdx.y;
     const bool valid = t < count;
@@ -110,7 +113,7 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __res
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < tile; k += DS_THREADS) {
             const uint32_t j = base + k;
-            double4 v = make_double4(0.0, 0.0, 0.0, 0.0);
+            Src v = {0.0, 0.0, 0.0, 0.0};
             if (j < j1) {
                 v.x = pos64[4 * (size_t)j];
                 v.y = pos64[4 * (size_t)j + 1];
@@ -122,7 +125,7 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __res
         __syncthreads();
         const uint32_t cnt = min(tile, j1 - base);
         for (uint32_t k = 0; k < cnt; ++k) {
-            const double4 s = s_src[k];
+            const Src s = s_src[k];
             if (s.w == 0.0) continue;
             const double rx = s.x - mx, ry = s.y - my, rz = s.z - mz;
             const double rr = rx * rx + ry * ry + rz * rz;
