@@ -237,6 +237,44 @@ def test_merge_and_oob_step(gbh_lib, oracle_mod):
     assert g.read_sim_values().out_of_bounds == o.read_sim_values().out_of_bounds
 
 
+def test_positions_in_order_after_merges(gbh_lib):
+    # After a graph step that merged, the next compaction reads the positions
+    # in order (kept current by the merge resolution); eager stage calls
+    # gather them through the index instead.  Both second steps must leave
+    # the same state bit for bit.
+    from gravity_gb300 import ic
+
+    n = 20000
+    b = ic.uniform_merge(n, seed=3)
+    b["pos_mass"][:, :3] *= 0.1
+    bounds = np.array([-2, -2, -2, 2, 2, 2], np.float32)
+    p = abi.step_params(dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+    sims = []
+    for _ in range(2):
+        sim = BarnesHut(n, bounds, abi.units(G=1.0))
+        sim.upload_bodies(b)
+        sim.init()
+        sim.step(p)
+        sims.append(sim)
+    a, g = sims
+    assert a.read_stats().merged > 50
+    a.step(p)  # graph: positions read in order
+    for stage in ("stage_reset", "stage_prepare"):
+        getattr(g, stage)(p)
+    g.stage_sort()
+    g.stage_build()
+    g.stage_fill()
+    g.stage_walk(p)
+    g.stage_merge(p)
+    g.stage_swap()
+    for x in (a, g):
+        x.synchronize()
+        assert x.read_stats().error_word == 0
+    assert a.read_sim_values().num_bodies == g.read_sim_values().num_bodies
+    assert np.array_equal(a.read_bodies().view(np.uint32), g.read_bodies().view(np.uint32))
+    assert np.array_equal(a.read_index(), g.read_index())
+
+
 def test_collision_mode_parity(gbh_lib, oracle_mod):
     from gravity_gb300 import ic
 
