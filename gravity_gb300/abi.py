@@ -220,7 +220,10 @@ def ic_params(kind, **kw) -> IcParams:
     if ranges is not None:
         for k, (lo, hi) in enumerate(ranges):
             p.lo[k], p.hi[k] = lo, hi
+    known = {f for f, _ in IcParams._fields_}
     for name, val in kw.items():
+        if name not in known:
+            raise TypeError(f"gbh_ic_params has no field {name!r}")
         if name in ("center", "velocity"):
             getattr(p, name)[:] = list(val)
         else:
