@@ -195,9 +195,10 @@ def max_over_ranks(dist, v: float, local) -> float:
 
 
 def cpu_baseline(wl, bodies, bounds, units, budget_s=20.0, threads=None):
-    """The reference algorithm (oracle port) on the host cores, on a bounded
-    sample: the full tree pipeline over all bodies plus the walk over every
-    `stride`-th body; steps/s extrapolates the walk to all bodies."""
+    """The reference algorithm (oracle port) on the host cores: whole steps of
+    BarnesHut.step (reset, compaction, bounds, encode, sort, build, fill, walk
+    over every body with the update, merge, swap), timed one after another
+    while the next step still fits the budget (at least one)."""
     from oracle import oracle as O
 
     if threads:
@@ -207,41 +208,30 @@ def cpu_baseline(wl, bodies, bounds, units, budget_s=20.0, threads=None):
     o.upload_bodies(bodies)
     o.init()
     p = wl["params"]
-    t0 = time.perf_counter()
-    o.stage_reset(p)
-    o.stage_prepare(p)
-    o.stage_sort()
-    o.stage_build()
-    o.stage_fill()
-    t_tree = time.perf_counter() - t0
-    n_live = o.read_sim_values().num_bodies
-    stride = 64
-    t0 = time.perf_counter()
-    inter = o.walk_sample(p, stride)
-    t_walk = time.perf_counter() - t0
-    sampled = (n_live + stride - 1) // stride
-    # grow the sample while it stays inside the budget
-    while t_tree + t_walk * 2 < budget_s and stride > 1:
-        stride //= 2
+    times = []
+    while not times or sum(times) + times[-1] < budget_s:
         t0 = time.perf_counter()
-        inter = o.walk_sample(p, stride)
-        t_walk = time.perf_counter() - t0
-        sampled = (n_live + stride - 1) // stride
-    t_walk_full = t_walk * n_live / max(sampled, 1)
+        o.step(p)
+        times.append(time.perf_counter() - t0)
+    st = o.read_stats()
     o.close()
+    total = sum(times)
     return {
-        "value": 1.0 / (t_tree + t_walk_full),
+        "value": len(times) / total,
         "unit": "steps/s",
         "cores": cores,
         "kind": "port",
-        "sample": f"tree pipeline over all {n_live} bodies ({t_tree:.2f} s) + walk over every {stride}-th body "
-                  f"({sampled} bodies, {t_walk:.2f} s, {inter} interactions), walk extrapolated to all bodies",
-        "t_tree_s": t_tree,
-        "t_walk_full_s": t_walk_full,
+        "sample": f"{len(times)} whole steps of the oracle over all {wl['n']} bodies (every body walked and "
+                  f"updated, no extrapolation), {total:.2f} s",
+        "s_per_step": total / len(times),
+        "interactions_per_step": int(st.interactions) // max(len(times), 1),
     }
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores (the oracle's C restatement
+    with OpenMP): every timed step is one whole BarnesHut.step over all bodies,
+    no sampling or extrapolation."""
     dist, rank, world, local = dist_setup()
     if rank != 0:
         return 0
@@ -256,20 +246,11 @@ def run_reference(args):
     o.upload_bodies(bodies)
     o.init()
     p = wl["params"]
-    n_live = wl["n"]
-    stride = args.ref_stride
 
     def one_step():
         t0 = time.perf_counter()
-        o.stage_reset(p)
-        o.stage_prepare(p)
-        o.stage_sort()
-        o.stage_build()
-        o.stage_fill()
-        t1 = time.perf_counter()
-        o.walk_sample(p, stride)
-        t2 = time.perf_counter()
-        return (t1 - t0) + (t2 - t1) * stride
+        o.step(p)
+        return time.perf_counter() - t0
 
     for _ in range(args.warmup):
         one_step()
@@ -296,8 +277,8 @@ def run_reference(args):
             "unit": "steps/s",
             "cores": O.get_threads(),
             "kind": "port",
-            "sample": f"each step: tree pipeline over all bodies + walk over every {stride}-th sorted body, "
-                      f"walk time scaled by {stride}",
+            "sample": "every step: one whole BarnesHut.step of the oracle over all bodies (reset, compaction, "
+                      "bounds, encode, sort, build, fill, walk and update of every body, merge, swap)",
         },
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -309,10 +290,9 @@ LEARNED_TAUS = [-3.0, -2.75, -2.6, -2.55, -2.5, -2.45, -2.4, -2.35, -2.3, -2.25,
 GROUP_THETAS = [0.4, 0.45, 0.5, 0.55, 0.6, 0.65, 0.7]
 PLAIN_THETAS = [0.3, 0.5, 0.7]
 # DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +
-# dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture
-# (profiles/walk_learned_mixture4M.md), divided by its bodies; the walk's
-# traffic grows in proportion to the bodies
-WALK_LEARNED_DRAM_BYTES_PER_BODY = 301.0  # learned walk DRAM read + write per body, 4M ncu capture
+# dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture,
+# divided by its bodies; the walk's traffic grows in proportion to the bodies
+WALK_LEARNED_DRAM_BYTES_PER_BODY = 301.0
 
 
 def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
@@ -424,6 +404,7 @@ def run_ours(args):
             calib["training"] = {"pairs": pairs, "epochs": args.mac_epochs, "loss_first": float(losses[0]),
                                  "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
         ref_sample = accuracy.DirectSumSample(bh, p_plain, count=4096, seed=2)
+        calib["judge"] = ref_sample.judge
         ref = {th: accuracy.evaluate(bh, ref_sample, plain(th)) for th in PLAIN_THETAS}
         head = accuracy.evaluate(bh, ref_sample, p_plain)
         target = head["p99"]
@@ -505,7 +486,8 @@ def run_ours(args):
     except (OSError, ValueError):
         peaks = {}
     sm_max = peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # FP32 FMA lanes x 2 flop x max SM clock
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * sm_max * 1e6 / 1e12  # FP32 FMA lanes x 2 flop x max SM clock
     walk_ms = stage_ms["walk"]
     walk_flop = WALK_FLOP_PER_INTERACTION * int(st_prof.interactions)
     mlp_flop = 2 * (12 * 32 + 32 * 32 + 32) * int(st_prof.mac_evaluations)
@@ -604,7 +586,8 @@ def run_ours(args):
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
             "traffic": traffic,
-            "peak_source": "152 SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json (of measured clock)",
+            "peak_source": f"{sm_count} SMs x 128 FP32 lanes x 2 flop x sm_max_mhz of MEASURED_PEAKS.json "
+                           "(of measured clock)",
             "flop_per_interaction": WALK_FLOP_PER_INTERACTION,
             "mlp_tflops": mlp_flop / (walk_ms / 1000.0) / 1e12,
         },
@@ -624,6 +607,23 @@ def run_ours(args):
         "stats": abi.stats_to_dict(st),
         "footprint_bytes": int(footprint),
     }
+    # last, so that a truncated view of the line keeps it
+    line["headline"] = {
+        "steps_per_s": value,
+        "e2e_steps_per_s": e2e["value"],
+        "judge": "fp64 direct sum, 4096 sampled bodies",
+        "plain_steps_per_s": compare.get("plain_theta", {}).get("steps_per_s"),
+        "plain_p99": compare.get("plain_theta", {}).get("p99"),
+        "learned_p99": compare.get("learned", {}).get("p99"),
+        "learned_speedup_vs_plain": compare.get("learned_speedup_vs_plain"),
+        "group_steps_per_s": compare.get("group_theta_ablation", {}).get("steps_per_s"),
+        "group_p99": compare.get("group_theta_ablation", {}).get("p99"),
+        "learned_weights": calib.get("weights_source"),
+        "cpu_steps_per_s": cpu["value"] if cpu else None,
+        "sm_count": sm_count,
+        "walk_frac_fp32": achieved / fp32_peak,
+        "sort_frac_hbm": sort_gbs / hbm_peak,
+    }
     print(json.dumps(line), flush=True)
     return 0
 
@@ -639,7 +639,6 @@ def main():
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--ref-stride", type=int, default=256)
     ap.add_argument("--plain-only", action="store_true", help="time the plain theta walk only")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain and group-theta comparison arms")
     ap.add_argument("--mac-weights", default=None, help="load MLP weights (.npy) instead of training")

@@ -41,6 +41,7 @@ MAC_FEATURES = 12
 MAC_HIDDEN = 32
 MAC_NUM_PARAMS = 32 * 12 + 32 + 32 * 32 + 32 + 32 + 1
 NONE_ID = 0xFFFFFFFF
+SORT_NOALLOC_MAX_PAIRS = 1 << 20  # GBH_SORT_NOALLOC_MAX_PAIRS
 
 BODY_DTYPE = np.dtype([("pos_mass", "<f4", (4,)), ("vel_density", "<f4", (4,))])
 NODE_DTYPE = np.dtype(

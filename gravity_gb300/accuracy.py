@@ -1,9 +1,9 @@
 """Acceleration error of a walk against the direct-sum reference, and matching of
 acceptance settings at equal p99 error.
 
-The reference (gbh_direct_sum) sums every body's pull on a seeded sample of bodies
-with FP32 terms and compensated sums (within ~1e-6 of an FP64 sum).  Errors
-are |a_walk - a_direct| / |a_direct| per sampled body.
+The judge (gbh_direct_sum) is an FP64 direct sum: every live body's pull on a
+seeded sample of bodies, FP64 terms and FP64 sums.  Errors are
+|a_walk - a_direct| / |a_direct| per sampled body.
 """
 from __future__ import annotations
 
@@ -24,7 +24,9 @@ def live_ids(sim) -> np.ndarray:
 
 
 class DirectSumSample:
-    """Direct-sum reference accelerations of a fixed sample of the current state."""
+    """FP64 direct-sum accelerations of a fixed sample of the current state."""
+
+    judge = "fp64"
 
     def __init__(self, sim, params: abi.StepParams, count: int = 4096, seed: int = 0):
         self.sample = sample_bodies(live_ids(sim), count, seed)

@@ -131,6 +131,7 @@ struct StepBuffers {
     uint32_t N;
     uint32_t sort_tiles_cap;
     uint32_t prep_tiles_cap;
+    uint32_t num_sms;  // multiprocessors of the context's device (grid sizes of the persistent kernels)
 };
 
 // ---- GLSL built-in semantics (GLSL 4.30 §8.3) -------------------------------
@@ -317,5 +318,3 @@ void launch_diagnostics(const gbh_body* bodies, uint32_t nb, const double* pos64
                         double* partial, uint32_t blocks, double* out, cudaStream_t s);
 void launch_merge(const StepBuffers& b, cudaStream_t s);
 void launch_init_index(uint32_t* idx, uint32_t N, gbh_sim_values* sim, const gbh_units* units_dev, cudaStream_t s);
-void launch_direct_sum(const gbh_body* bodies, uint32_t n_bodies, const uint32_t* sample, uint32_t count,
-                       float G, float soft, double* partial, double* out, uint32_t chunks, cudaStream_t s);

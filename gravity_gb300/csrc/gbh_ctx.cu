@@ -100,6 +100,7 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.N = c->N;
     b.sort_tiles_cap = c->sort_tiles_cap;
     b.prep_tiles_cap = c->prep_tiles_cap;
+    b.num_sms = c->num_sms;
     return b;
 }
 
@@ -261,8 +262,14 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     e = cudaSetDevice(device);
     if (e != cudaSuccess) return fail(nullptr, GBH_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
 
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess || sms <= 0)
+        return fail(nullptr, GBH_ERR_CUDA, std::string("multiprocessor count: ") + cudaGetErrorString(e));
+
     gbh_ctx* c = new gbh_ctx();
     c->device = device;
+    c->num_sms = (uint32_t)sms;
     c->N = n;
     c->prep_tiles_cap = (n + PREP_TILE - 1) / PREP_TILE;
     c->sort_tiles_cap = (n + SORT_TILE - 1) / SORT_TILE;
@@ -334,6 +341,9 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     group_walk_setup();
     fill_setup();
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+    for (cudaEvent_t& ev : c->copy_events)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->arena, 0, A.total, c->stream);
     // SimulationValues as packed by GPU.packValues (GPU.java:1096-1143)
     gbh_sim_values sv;
@@ -403,10 +413,6 @@ int gbh_exchange_bodies(gbh_ctx* c, gbh_body* host_out, const gbh_body* host_in,
     if (!count) return GBH_OK;
     CUDA_TRY(c, cudaSetDevice(c->device));
     constexpr uint32_t CHUNKS = sizeof(c->copy_events) / sizeof(c->copy_events[0]);
-    if (!c->copy_stream) {
-        CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        for (cudaEvent_t& e : c->copy_events) CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
     gbh_body* dev = c->bodies[c->bin] + offset;
     // the read-back starts once the work queued so far (the last step) is done
     CUDA_TRY(c, cudaEventRecord(c->copy_events[0], c->stream));
@@ -638,7 +644,7 @@ int gbh_read_diagnostics(gbh_ctx* c, gbh_diagnostics* out) {
     CUDA_TRY(c, cudaSetDevice(c->device));
     const bool pot = c->potential && c->potential_epoch == c->state_epoch;
     const bool p64 = c->pos64[0] && c->pos64_valid;
-    const uint32_t blocks = 152 * 4;
+    const uint32_t blocks = c->num_sms * 4;
     double* d = nullptr;
     CUDA_TRY(c, cudaMalloc(&d, (size_t)(blocks + 1) * 16 * 8));
     launch_diagnostics(c->bodies[c->bin], c->N, p64 ? c->pos64[c->bin] : nullptr, pot ? c->potential : nullptr,
@@ -821,7 +827,7 @@ int gbh_direct_sum(gbh_ctx* c, const gbh_step_params* p, const uint32_t* sample,
     int rc = read_dev(c, &sv, c->sim, sizeof(sv));
     if (rc) return rc;
     const uint32_t blocks = (count + 127) / 128;
-    uint32_t chunks = (152 * 16 + blocks - 1) / blocks;
+    uint32_t chunks = (c->num_sms * 16 + blocks - 1) / blocks;
     if (chunks < 1) chunks = 1;
     if (chunks > c->N) chunks = c->N;
     uint32_t* d_sample = nullptr;
@@ -830,14 +836,12 @@ int gbh_direct_sum(gbh_ctx* c, const gbh_step_params* p, const uint32_t* sample,
     CUDA_TRY(c, cudaMalloc(&d_partial, (size_t)chunks * count * 3 * 8));
     CUDA_TRY(c, cudaMalloc(&d_out, (size_t)count * 3 * 8));
     cudaError_t e = cudaMemcpyAsync(d_sample, sample, (size_t)count * 4, cudaMemcpyHostToDevice, c->stream);
-    const bool fp64 = p->precision_mode == GBH_PRECISION_COMPENSATED && c->pos64_valid;
+    // FP64 positions of the precision form when they hold the current state,
+    // else the FP32 positions widened
+    const bool pos64 = p->precision_mode == GBH_PRECISION_COMPENSATED && c->pos64_valid;
     if (e == cudaSuccess) {
-        if (fp64)
-            launch_direct_sum64(c->pos64[c->bin], c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant,
-                                p->softening, d_partial, d_out, chunks, c->stream);
-        else
-            launch_direct_sum(c->bodies[c->bin], c->N, d_sample, count, sv.gravitational_constant, p->softening,
-                              d_partial, d_out, chunks, c->stream);
+        launch_direct_sum64(pos64 ? c->pos64[c->bin] : nullptr, c->bodies[c->bin], c->N, d_sample, count,
+                            sv.gravitational_constant, p->softening, d_partial, d_out, chunks, c->stream);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, (size_t)count * 3 * 8, cudaMemcpyDeviceToHost, c->stream);

@@ -10,6 +10,7 @@ struct MacState;  // learned MAC buffers (k_mac.cu)
 
 struct gbh_ctx {
     int device = 0;
+    uint32_t num_sms = 1;  // cudaDevAttrMultiProcessorCount of `device`
     cudaStream_t stream = nullptr;
     uint32_t N = 0;
     uint32_t prep_tiles_cap = 0;
@@ -71,7 +72,7 @@ struct gbh_ctx {
     MacState* mac = nullptr;
 
     // gbh_exchange_bodies: a second stream for the device-to-host half and
-    // one event per chunk (created on first use)
+    // one event per chunk (created with the context)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_events[16] = {};
 

@@ -1,13 +1,12 @@
-// k_diag.cu — the accuracy reference (direct-sum accelerations of sampled bodies),
+// k_diag.cu — the accuracy reference (an FP64 direct sum of sampled bodies),
 // the FP64 diagnostics of conserved quantities, and the FP64 positions of the
 // precision form.
 //
 // The reference has no accuracy check.  The direct sum adds G m_j r / (r.r + eps^2)^1.5
-// over every live body j != i for a sample of bodies i.  Each term is computed
-// in FP32 (the positions are FP32, so r = x_j - x_i carries one rounding) and
-// the sums are carried in double-float (TwoSum compensation), so the result
-// matches an FP64 direct sum to ~1e-6 relative while running at FP32 rate
-// (the GB300's FP64 rate is 1/64 of FP32).
+// over every live body j != i for a sample of bodies i, with FP64 terms and
+// FP64 sums: positions come from the precision form's FP64 copy when it is
+// current, otherwise the FP32 body positions widened to FP64 (exactly).  This
+// is the judge every acceleration-error distribution is measured against.
 //
 // Grid: (sample blocks) x (source chunks).  Each block keeps 128 targets in
 // registers and streams its chunk of sources through shared memory; partial
@@ -16,57 +15,6 @@
 
 #define DS_THREADS 128
 #define DS_TILE 512
-
-__device__ __forceinline__ void two_sum(float& hi, float& lo, float x) {
-    const float s = hi + x;
-    const float bp = s - hi;
-    const float err = (hi - (s - bp)) + (x - bp);
-    hi = s;
-    lo = lo + err;
-}
-
-__global__ __launch_bounds__(DS_THREADS) void k_direct_sum(const gbh_body* __restrict__ bodies, uint32_t nb,
-                                                           const uint32_t* __restrict__ sample, uint32_t count, float G,
-                                                           float soft, uint32_t chunks, double* __restrict__ partial) {
-    __shared__ float4 s_src[DS_TILE];
-    const uint32_t t = blockIdx.x * DS_THREADS + threadIdx.x;
-    const uint32_t chunk = blockIdx.y;
-    const bool valid = t < count;
-    const uint32_t i = valid ? sample[t] : 0u;
-    const float4 me = valid ? ld_pos_mass(bodies, i) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const uint32_t per = (nb + chunks - 1) / chunks;
-    const uint32_t j0 = chunk * per;
-    const uint32_t j1 = min(nb, j0 + per);
-    float hx = 0.f, lx = 0.f, hy = 0.f, ly = 0.f, hz = 0.f, lz = 0.f;
-    for (uint32_t base = j0; base < j1; base += DS_TILE) {
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < DS_TILE; k += DS_THREADS) {
-            const uint32_t j = base + k;
-            s_src[k] = j < j1 ? ld_pos_mass(bodies, j) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        __syncthreads();
-        const uint32_t cnt = min((uint32_t)DS_TILE, j1 - base);
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const float4 s = s_src[k];
-            if (s.w == 0.0f) continue;
-            const float rx = s.x - me.x, ry = s.y - me.y, rz = s.z - me.z;
-            const float rr = rx * rx + ry * ry + rz * rz;
-            if (rr == 0.0f) continue;  // the body itself (a zero vector adds nothing)
-            const float d2 = rr + soft;
-            const float inv = 1.0f / sqrtf(d2);
-            const float f = G * s.w * inv * inv * inv;
-            two_sum(hx, lx, f * rx);
-            two_sum(hy, ly, f * ry);
-            two_sum(hz, lz, f * rz);
-        }
-    }
-    if (valid) {
-        double* o = partial + ((size_t)chunk * count + t) * 3;
-        o[0] = (double)hx + (double)lx;
-        o[1] = (double)hy + (double)ly;
-        o[2] = (double)hz + (double)lz;
-    }
-}
 
 __global__ void k_direct_sum_reduce(const double* __restrict__ partial, uint32_t count, uint32_t chunks,
                                     double* __restrict__ out) {
@@ -77,17 +25,10 @@ __global__ void k_direct_sum_reduce(const double* __restrict__ partial, uint32_t
     out[t] = s;
 }
 
-void launch_direct_sum(const gbh_body* bodies, uint32_t nb, const uint32_t* sample, uint32_t count, float G,
-                       float soft, double* partial, double* out, uint32_t chunks, cudaStream_t s) {
-    dim3 grid((count + DS_THREADS - 1) / DS_THREADS, chunks);
-    k_direct_sum<<<grid, DS_THREADS, 0, s>>>(bodies, nb, sample, count, G, soft, chunks, partial);
-    k_direct_sum_reduce<<<(3 * count + 255) / 256, 256, 0, s>>>(partial, count, chunks, out);
-}
-
 // ---------------------------------------------------------------------------
-// FP64 direct sum of the precision form: positions from the FP64 copy, terms
-// and sums in FP64 (the GB300 runs FP64 at a fraction of the FP32 rate; the
-// reference samples a few thousand bodies).
+// FP64 direct sum: positions from the FP64 copy (pos64 != null) or the FP32
+// body positions widened, terms and sums in FP64 (the GB300 runs FP64 at a
+// fraction of the FP32 rate; the judge samples a few thousand bodies).
 __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __restrict__ pos64,
                                                              const gbh_body* __restrict__ bodies, uint32_t nb,
                                                              const uint32_t* __restrict__ sample, uint32_t count,
@@ -101,9 +42,17 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __res
     const uint32_t chunk = blockIdx.y;
     const bool valid = t < count;
     const uint32_t i = valid ? sample[t] : 0u;
-    const double mx = valid ? pos64[4 * (size_t)i] : 0.0;
-    const double my = valid ? pos64[4 * (size_t)i + 1] : 0.0;
-    const double mz = valid ? pos64[4 * (size_t)i + 2] : 0.0;
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    if (valid && pos64) {
+        mx = pos64[4 * (size_t)i];
+        my = pos64[4 * (size_t)i + 1];
+        mz = pos64[4 * (size_t)i + 2];
+    } else if (valid) {
+        const float4 pm = ld_pos_mass(bodies, i);
+        mx = pm.x;
+        my = pm.y;
+        mz = pm.z;
+    }
     const uint32_t per = (nb + chunks - 1) / chunks;
     const uint32_t j0 = chunk * per;
     const uint32_t j1 = min(nb, j0 + per);
@@ -115,10 +64,17 @@ __global__ __launch_bounds__(DS_THREADS) void k_direct_sum64(const double* __res
             const uint32_t j = base + k;
             Src v = {0.0, 0.0, 0.0, 0.0};
             if (j < j1) {
-                v.x = pos64[4 * (size_t)j];
-                v.y = pos64[4 * (size_t)j + 1];
-                v.z = pos64[4 * (size_t)j + 2];
-                v.w = (double)ld_pos_mass(bodies, j).w;
+                const float4 pm = ld_pos_mass(bodies, j);
+                if (pos64) {
+                    v.x = pos64[4 * (size_t)j];
+                    v.y = pos64[4 * (size_t)j + 1];
+                    v.z = pos64[4 * (size_t)j + 2];
+                } else {
+                    v.x = pm.x;
+                    v.y = pm.y;
+                    v.z = pm.z;
+                }
+                v.w = (double)pm.w;
             }
             s_src[k] = v;
         }

@@ -163,7 +163,7 @@ __global__ void k_merge_clear(StepBuffers b) {
 }
 
 void launch_merge(const StepBuffers& b, cudaStream_t s) {
-    const uint32_t blocks = 152 * 4;
+    const uint32_t blocks = b.num_sms * 4;
     k_merge_count<<<blocks, 256, 0, s>>>(b);
     k_merge_apply<<<blocks, 256, 0, s>>>(b);
     k_merge_conflicts<<<1, MERGE_SORT_THREADS, 0, s>>>(b);

@@ -5,8 +5,8 @@
 // a host whose device memory is owned by another allocator (a Java or game
 // engine renderer that hands out only its own buffers), code that runs while
 // another component holds the device's memory pool, or a hot loop that must
-// never hit the allocator's locks or device synchronisation.  It sorts
-// (uint64 key, uint32 value) pairs that the caller already has on the device.
+// never hit the allocator's locks.  It sorts (uint64 key, uint32 value) pairs
+// that the caller already has on the device.
 //
 // Scratch: everything the onesweep sort needs beyond the caller's inputs and
 // outputs (a ping-pong copy of the pairs, the digit histograms, the look-back
@@ -16,9 +16,15 @@
 // start at zero, and calls that overlap on the GPU (on different streams or
 // threads) race on it; serialise them.
 //
-// The device address of the array is taken once per device, with that device
-// current, by the first call on that device (cudaGetSymbolAddress).  Make
-// that first call before any stream capture.
+// Set-up, once per device, by the first call with that device current: the
+// array's device address (cudaGetSymbolAddress), the sort kernels' shared
+// memory limits and the multiprocessor count.  Make that first call before
+// any stream capture.  Every call ends by reading the device error word and
+// synchronising its stream, so no call can be captured in a CUDA graph.
+// The cached address belongs to the device's current context: after a
+// cudaDeviceReset of that device the library must not be used again in the
+// same process.
+#include <cstring>
 #include <mutex>
 
 #include "gbh_common.cuh"
@@ -40,7 +46,11 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_sort_scratch;
 
-static NoAllocScratch* g_scratch_ptr[NOALLOC_MAX_DEVICES];
+struct NoAllocDevice {
+    NoAllocScratch* scratch = nullptr;  // device address of g_sort_scratch
+    uint32_t num_sms = 0;
+};
+static NoAllocDevice g_dev[NOALLOC_MAX_DEVICES];
 static std::mutex g_scratch_mu;
 
 // digit histograms of all 8 passes and the live count, into the scratch
@@ -59,23 +69,30 @@ __global__ void k_noalloc_hist(const uint64_t* __restrict__ keys, uint32_t n, No
         if (h[i]) atomicAdd(&s->hist[i], h[i]);
 }
 
-static NoAllocScratch* scratch_for_current_device(int* status) {
+// The set-up of the current device, done once: the scratch's device address,
+// the sort kernels' attributes and the multiprocessor count.
+static const NoAllocDevice* setup_current_device(int* status) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
         *status = GBH_ERR_CUDA;
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    NoAllocDevice& d = g_dev[dev];
+    if (!d.scratch) {
         void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_sort_scratch) != cudaSuccess || !p) {
+        int sms = 0;
+        if (cudaGetSymbolAddress(&p, g_sort_scratch) != cudaSuccess || !p ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
             *status = GBH_ERR_CUDA;
             return nullptr;
         }
-        g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
+        sort_setup();
+        d.num_sms = (uint32_t)sms;
+        d.scratch = static_cast<NoAllocScratch*>(p);
     }
     *status = GBH_OK;
-    return g_scratch_ptr[dev];
+    return &d;
 }
 
 extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
@@ -83,9 +100,19 @@ extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* v
     if (n > NOALLOC_MAX_PAIRS) return GBH_ERR_INVALID;
     if (n == 0) return GBH_OK;
     if (!keys_in || !vals_in || !keys_out || !vals_out) return GBH_ERR_INVALID;
+    // outputs either are the inputs (sorted in place) or do not overlap them
+    const char *ki = (const char*)keys_in, *ko = (const char*)keys_out;
+    const char *vi = (const char*)vals_in, *vo = (const char*)vals_out;
+    if ((ko != ki && ko < ki + (size_t)n * 8 && ki < ko + (size_t)n * 8) ||
+        (vo != vi && vo < vi + (size_t)n * 4 && vi < vo + (size_t)n * 4))
+        return GBH_ERR_INVALID;
     int status = GBH_OK;
-    NoAllocScratch* s = scratch_for_current_device(&status);
-    if (!s) return status;
+    const NoAllocDevice* dv = setup_current_device(&status);
+    if (!dv) return status;
+    NoAllocScratch* s = dv->scratch;
+    // a launch error pending from earlier work of this thread is cleared here,
+    // so that the check after the launches below reports this call's own
+    (void)cudaGetLastError();
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the sort runs in place in the caller's output buffers
     if (keys_out != keys_in &&
@@ -102,7 +129,7 @@ extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* v
         if (cudaMemsetAsync(s->lookback + (size_t)p * NOALLOC_TILES * SORT_RADIX, 0, (size_t)tiles * SORT_RADIX * 4,
                             st) != cudaSuccess)
             return GBH_ERR_CUDA;
-    const uint32_t hblocks = min((n + 255) / 256, 152u * 4u);
+    const uint32_t hblocks = min((n + 255) / 256, dv->num_sms * 4u);
     k_noalloc_hist<<<hblocks, 256, 0, st>>>(keys_out, n, s);
     StepBuffers b;
     memset(&b, 0, sizeof(b));
@@ -116,7 +143,7 @@ extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* v
     b.lookback = s->lookback;
     b.N = n;
     b.sort_tiles_cap = NOALLOC_TILES;
-    sort_setup();
+    b.num_sms = dv->num_sms;
     launch_sort(b, st);
     if (cudaGetLastError() != cudaSuccess) return GBH_ERR_CUDA;
     // report errors raised on the device (bounded look-back waits)

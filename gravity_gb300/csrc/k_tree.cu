@@ -465,5 +465,5 @@ void fill_setup() {
 
 void launch_fill(const StepBuffers& b, cudaStream_t s) {
     k_fill<<<(b.N + FILL_TILE - 1) / FILL_TILE, FILL_TILE, FILL_SMEM, s>>>(b);
-    k_fill_top<<<152 * 4, 256, 0, s>>>(b);
+    k_fill_top<<<b.num_sms * 4, 256, 0, s>>>(b);
 }

@@ -317,11 +317,12 @@ int gbh_stage_swap(gbh_ctx* ctx);
 int gbh_step_profiled(gbh_ctx* ctx, const gbh_step_params* params, float ms_out[GBH_NUM_STAGES]);
 
 /* ---- accuracy reference -------------------------------------------------------
- * Direct-sum accelerations for `count` sampled body indices against every live
- * body of the current state (terms in FP32, sums compensated in double-float).
- * out: double[3*count].  Uses G, softening from `params`. */
-/* With params->precision_mode == GBH_PRECISION_COMPENSATED and current FP64
- * positions, the terms and sums are FP64 throughout (an FP64 direct sum). */
+ * FP64 direct-sum accelerations for `count` sampled body indices against every
+ * live body of the current state: FP64 terms and FP64 sums, reduced in a fixed
+ * order.  Positions are the FP32 body positions widened to FP64, or, with
+ * params->precision_mode == GBH_PRECISION_COMPENSATED and current FP64
+ * positions, the FP64 positions.  out: double[3*count].  Uses G and softening
+ * from `params`. */
 int gbh_direct_sum(gbh_ctx* ctx, const gbh_step_params* params, const uint32_t* sample,
                    uint32_t count, double* out_accel);
 
@@ -366,22 +367,28 @@ int gbh_mac_predict(gbh_ctx* ctx, const float* features, uint32_t count, float* 
  * No counterpart in the reference: this entry point is new in this library.
  * For callers that cannot call cudaMalloc — a host whose device memory belongs
  * to another allocator or engine, code running while another component owns
- * the memory pool, or a loop that must never take the allocator's locks or
- * synchronise the device.  Stable ascending sort of n (uint64 key, uint32
- * value) pairs by key, on device memory the caller provides (inputs and
- * outputs may alias; the inputs are left untouched when they do not).  The
- * same onesweep kernels as the step's sort.
+ * the memory pool, or a loop that must never take the allocator's locks.
+ * Stable ascending sort of n (uint64 key, uint32 value) pairs by all 64 key
+ * bits, on device memory the caller provides.  Each output buffer is either
+ * identical to its input (sorted in place) or disjoint from it; partly
+ * overlapping buffers return GBH_ERR_INVALID.  Disjoint inputs are left
+ * untouched.  The same onesweep kernels as the step's sort.
  *   - n is at most 1,048,576 (GBH_SORT_NOALLOC_MAX_PAIRS); larger n returns
  *     GBH_ERR_INVALID.
  *   - Allocates nothing: its scratch (about 15 MB) is a static device array
  *     that every GPU loading this library holds until exit, shared by all
  *     calls.  Each call clears what must start at zero; calls that overlap on
  *     the GPU race on the scratch and must be serialised by the caller.
- *   - The first call on a device looks up the scratch's device address with
- *     that device current; make that first call before any stream capture.
+ *   - The first call on a device does its set-up (the scratch's device
+ *     address, with that device current); make that first call before any
+ *     stream capture.  The library must not be used again on a device after a
+ *     cudaDeviceReset of it.
  *   - Runs on `stream` (a cudaStream_t, NULL = default stream) on the current
- *     device and returns after the sort has finished; GBH_ERR_DEVICE when a
- *     bounded wait of the sort gave up. */
+ *     device, reads the device error word and synchronises `stream` before
+ *     it returns, so it cannot be captured in a CUDA graph.  GBH_ERR_DEVICE
+ *     when a bounded wait of the sort gave up.
+ *   - Clears the calling thread's pending CUDA launch error at entry, so that
+ *     GBH_ERR_CUDA reports a failure of this call's own launches. */
 #define GBH_SORT_NOALLOC_MAX_PAIRS (1u << 20)
 int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                            uint32_t* vals_out, uint32_t n, void* stream);

@@ -22,7 +22,9 @@ from gravity_gb300 import abi
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_ref", "libbh_ref.so")
-REF_SHADERS = "/root/reference/src/main/resources/shaders"
+# the reference checkout: GBH_REFERENCE (default: where this container mounts it)
+REF_ROOT = os.environ.get("GBH_REFERENCE", "/root/reference")
+REF_SHADERS = os.path.join(REF_ROOT, "src", "main", "resources", "shaders")
 _lib = None
 
 

@@ -2,11 +2,15 @@
 
 The harness (oracle/ref_glsl, oracle/ref_harness.py) runs the reference's own
 GLSL compute kernels compiled as C++; it exists only where the reference
-sources are mounted.  Each fixture stores its input bodies, bounds, units and
-step parameters and the reference's outputs, so tests can check the CPU oracle
-and the GPU path against the reference anywhere.
+sources are mounted.  Each small fixture (1,024 bodies) stores its input
+bodies, bounds, units and step parameters and the reference's outputs, so
+tests can check the CPU oracle and the GPU path against the reference
+anywhere.  The large fixtures (large_*.npz, 65,536 bodies: 16 tiles of the
+GPU sort, about 128 tiles of its fill) store the generator of their inputs
+(tests/golden/large_inputs.py) with a digest of the bodies, digests of the
+reference's exact outputs, and every 16th body after the step.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--large-only]
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ sys.path.insert(0, ROOT)
 
 from gravity_gb300 import abi, ic  # noqa: E402
 from oracle import ref_harness as R  # noqa: E402
+from tests.golden import large_inputs as L  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 
@@ -63,8 +68,69 @@ def cases():
         dt=1e-3, theta=0.5, softening=1e-2, bounds=abi.BOUNDS_STATIC), 1
 
 
+LARGE_N = 65536
+
+
+def large_cases():
+    yield "large_clusters_dynamic", ("clusters", LARGE_N, 21), None, abi.step_params(
+        dt=1e-3, theta=0.5, softening=1e-4, bounds=abi.BOUNDS_DYNAMIC)
+    yield "large_merge_static", ("merge_box", LARGE_N, 22), np.array([-2, -2, -2, 2, 2, 2], np.float32), \
+        abi.step_params(dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+
+
+def make_large():
+    units = abi.units(G=1.0)
+    for name, (kind, n, seed), bounds, p in large_cases():
+        bodies = L.make(kind, n, seed)
+        if bounds is None:
+            bounds = live_bounds(bodies)
+        r = R.RefBarnesHut(n, bounds, units)
+        r.upload_bodies(bodies)
+        r.init()
+        r.stage_reset(p)
+        r.stage_prepare(p)
+        s = r.read_sim_values()
+        nl = s.num_bodies
+        out = {"kind": np.array(kind), "n": n, "seed": seed, "input_sha256": np.array(L.digest(bodies)),
+               "bounds": bounds, "params": np.array([float(getattr(p, f)) for f in PARAM_FIELDS]),
+               "prep_num_bodies": nl,
+               "prep_bounds": np.array(list(s.bounds_min) + list(s.bounds_max), np.float32),
+               "prep_index": np.array(L.digest(r.read_index())),
+               "prep_morton": np.array(L.digest(r.read_morton()[:nl]))}
+        r.stage_sort()
+        r.stage_build()
+        r.stage_fill()
+        r.stage_walk(p)
+        tasks = r.read_merge_tasks()
+        out["tasks"] = np.array(L.task_digest(tasks))
+        out["task_count"] = len(tasks)
+        r.stage_merge(p)
+        r.stage_swap()
+        out["sorted_index"] = np.array(L.digest(r.read_index()[:nl]))
+        out["sorted_morton"] = np.array(L.digest(r.read_morton()[:nl]))
+        for f, d in L.node_digests(r.read_internal_nodes()[: max(nl - 1, 1)]).items():
+            out[f"internal_{f}"] = np.array(d)
+        for f, d in L.node_digests(r.read_leaf_nodes()[:nl]).items():
+            out[f"leaf_{f}"] = np.array(d)
+        after = r.read_bodies()
+        out["bodies_after"] = np.array(L.digest(after.view(np.float32)))
+        out["bodies_sample"] = after[::16].copy()
+        out["dead_after"] = np.array(L.digest((after["pos_mass"][:, 3] == 0).astype(np.uint8)))
+        sv = r.read_sim_values()
+        out["uint_debug0"] = sv.uint_debug[0]
+        out["out_of_bounds"] = sv.out_of_bounds
+        r.close()
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(path, os.path.getsize(path), "tasks", len(tasks))
+
+
 def main():
     units = abi.units(G=1.0)
+    if "--large-only" in sys.argv:
+        make_large()
+        return
+    make_large()
     for name, bodies, bounds, p, steps in cases():
         if bounds is None:
             bounds = live_bounds(bodies)

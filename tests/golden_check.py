@@ -24,7 +24,13 @@ def same_bits(a, b) -> bool:
 
 
 def fixtures():
-    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
+    """The small fixtures (inputs and outputs stored whole)."""
+    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")) if not os.path.basename(p).startswith("large_"))
+
+
+def large_fixtures():
+    """The large fixtures (generated inputs, digests of the outputs)."""
+    return sorted(glob.glob(os.path.join(GOLDEN_DIR, "large_*.npz")))
 
 
 def params_of(z) -> abi.StepParams:
@@ -91,4 +97,55 @@ def replay(path, make, exact_walk: bool, ordered_tasks: bool):
             # later steps start from the reference's state so that each step is compared on equal inputs
             x.upload_bodies(gb)
         assert x.read_sim_values().out_of_bounds == int(z[pre + "out_of_bounds"]), path
+    return True
+
+
+def replay_large(path, make, exact_walk: bool):
+    """One step of a large fixture: inputs regenerated (digest checked), every
+    exact output compared by digest; bodies after the step bit-identical
+    (exact_walk) or, on every 16th body, within 1e-5."""
+    from tests.golden import large_inputs as L
+
+    z = np.load(path)
+    kind, n, seed = str(z["kind"]), int(z["n"]), int(z["seed"])
+    bodies = L.make(kind, n, seed)
+    assert L.digest(bodies) == str(z["input_sha256"]), (path, "regenerated inputs differ")
+    p = params_of(z)
+    x = make(n, z["bounds"], abi.units(G=1.0))
+    x.upload_bodies(bodies)
+    x.init()
+    x.stage_reset(p)
+    x.stage_prepare(p)
+    s = x.read_sim_values()
+    nl = s.num_bodies
+    assert nl == int(z["prep_num_bodies"]), path
+    assert np.array_equal(np.array(list(s.bounds_min) + list(s.bounds_max), np.float32), z["prep_bounds"]), path
+    assert L.digest(x.read_index()) == str(z["prep_index"]), path
+    assert L.digest(x.read_morton()[:nl]) == str(z["prep_morton"]), path
+    x.stage_sort()
+    x.stage_build()
+    x.stage_fill()
+    x.stage_walk(p)
+    tasks = x.read_merge_tasks()
+    assert len(tasks) == int(z["task_count"]), path
+    assert L.task_digest(tasks) == str(z["tasks"]), path
+    x.stage_merge(p)
+    x.stage_swap()
+    assert L.digest(x.read_index()[:nl]) == str(z["sorted_index"]), path
+    assert L.digest(x.read_morton()[:nl]) == str(z["sorted_morton"]), path
+    for f, d in L.node_digests(x.read_internal_nodes()[: max(nl - 1, 1)]).items():
+        assert d == str(z[f"internal_{f}"]), (path, "internal", f)
+    for f, d in L.node_digests(x.read_leaf_nodes()[:nl]).items():
+        assert d == str(z[f"leaf_{f}"]), (path, "leaf", f)
+    after = x.read_bodies()
+    assert L.digest((after["pos_mass"][:, 3] == 0).astype(np.uint8)) == str(z["dead_after"]), path
+    if exact_walk:
+        assert L.digest(after.view(np.float32)) == str(z["bodies_after"]), path
+        assert x.read_sim_values().uint_debug[0] == int(z["uint_debug0"]), path
+    else:
+        gb = z["bodies_sample"]
+        mine = after[::16]
+        np.testing.assert_allclose(mine["pos_mass"], gb["pos_mass"], rtol=1e-5, atol=1e-6, equal_nan=True)
+        np.testing.assert_allclose(mine["vel_density"], gb["vel_density"], rtol=1e-4, atol=1e-5, equal_nan=True)
+    assert x.read_sim_values().out_of_bounds == int(z["out_of_bounds"]), path
     return True

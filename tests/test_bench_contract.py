@@ -26,7 +26,7 @@ def _run(args, env=None, timeout=300):
 
 def test_reference_arm_json_line():
     r = _run(["bench.py", "--impl", "reference", "--workload", "plummer", "--n", "4096", "--steps", "1",
-              "--warmup", "0", "--ref-stride", "16"])
+              "--warmup", "0"])
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
@@ -37,13 +37,14 @@ def test_reference_arm_json_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "steps/s"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert "extrapolat" not in d["cpu_baseline"]["sample"]  # whole steps, measured
 
 
 def test_reference_arm_two_ranks_one_line():
     port = _free_port()
     r = _run(["-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2", "--master-addr", "127.0.0.1",
               "--master-port", str(port), "bench.py", "--impl", "reference", "--workload", "plummer",
-              "--steps", "1", "--warmup", "0", "--ref-stride", "64"],
+              "--steps", "1", "--warmup", "0"],
              env={"GBH_BENCH_BACKEND": "gloo", "OMP_NUM_THREADS": "2"})
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]

@@ -302,4 +302,5 @@ def test_direct_sum_matches_fp64(gbh_lib, oracle_mod):
     sample = np.arange(0, n, 97, dtype=np.uint32)
     got = g.direct_sum(p, sample)
     ref = oracle_mod.direct_sum_fp64(b, sample, 1.0, 1e-4)
-    assert rel_err(got, ref).max() < 1e-5
+    # both FP64 throughout: only the summation order differs
+    assert rel_err(got, ref).max() < 1e-11
