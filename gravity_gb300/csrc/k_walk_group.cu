@@ -30,12 +30,19 @@
 #include "gbh_ctx.h"
 #include "mac_mlp.cuh"
 
+#ifndef GW_THREADS
 #define GW_THREADS 256
+#endif
 #define GW_WARPS (GW_THREADS / 32)
 #define GW_STACK 768
 #define GW_LIST 64
 #define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
 #define GW_BPL (GBH_GROUP_MAX / 32)  // bodies per lane
+#ifdef GW_MINB_ALL
+#define GW_MINB(MODE, FORM) GW_MINB_ALL
+#else
+#define GW_MINB(MODE, FORM) (((MODE) == GM_THETA && (FORM) == FORM_FP32) ? 3 : 2)
+#endif
 
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 
@@ -45,7 +52,10 @@ enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 template <int STACK>
 struct GroupSmem {
     uint32_t stack[GW_WARPS][STACK];
-    float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
+    // list entries (centre of mass, G x mass), each value stored twice:
+    // [0] = (x, x, y, y), [1] = (z, z, w, w), so that one 128-bit load gives
+    // the packed pairs the FP32x2 force loop takes as operands
+    float4 list_cm[GW_WARPS][GW_LIST][2];
     uint32_t list_id[GW_WARPS][GW_LIST];
     float list_rad[GW_WARPS][GW_LIST];  // merge form: the leaf entries' body radii
     // merge form: each group body's radius and task counter (slot q * 32 +
@@ -70,6 +80,18 @@ struct GroupCfg {
     using Smem = GroupSmem<stack>;
     static constexpr size_t smem = MODE == GM_LEARNED ? sizeof(Smem) : offsetof(Smem, pend_cm);
 };
+
+// A lane's three body slots, stored so that slots 0 and 1 form packed FP32x2
+// pairs (one __ffma2_rn serves both) and slot 2 stands alone.  Positions are
+// kept negated: r = c + (-x) is one add.
+static_assert(GW_BPL == 3, "the packed layout holds three body slots per lane");
+struct Slots3 {
+    float2 x01, y01, z01;
+    float x2, y2, z2;
+};
+__device__ __forceinline__ float& sx(Slots3& a, int q) { return q == 0 ? a.x01.x : q == 1 ? a.x01.y : a.x2; }
+__device__ __forceinline__ float& sy(Slots3& a, int q) { return q == 0 ? a.y01.x : q == 1 ? a.y01.y : a.y2; }
+__device__ __forceinline__ float& sz(Slots3& a, int q) { return q == 0 ? a.z01.x : q == 1 ? a.z01.y : a.z2; }
 
 // Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
 // more (every leaf lies in exactly one).  A group is a contiguous range of
@@ -134,7 +156,7 @@ __global__ void k_find_groups(StepBuffers b) {
 enum GroupForm { FORM_FP32 = 0, FORM_PREC = 1, FORM_MERGE = 2 };
 
 template <int MODE, int FORM>
-__global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32) ? 3 : 2) void k_walk_group(
+__global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
     StepBuffers b, MacDeviceWeights mw) {
     constexpr bool PREC = FORM == FORM_PREC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -166,7 +188,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     const float G = sim->gravitational_constant;
     const float soft = P->softening, theta = P->theta, tol = P->mac_tolerance;
     uint32_t* stk = S.stack[w];
-    float4* lcm = S.list_cm[w];
+    float4(*lcm)[2] = S.list_cm[w];
     uint32_t* lid = S.list_id[w];
     float* lrad = S.list_rad[w];
 
@@ -211,15 +233,19 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         __syncwarp();
     }
 
-    // walk coordinates of this lane's bodies (absolute, or group-relative)
-    float3 pw[GW_BPL];
+    // walk coordinates of this lane's bodies (absolute, or group-relative),
+    // negated
+    Slots3 np_;
 #pragma unroll
     for (int q = 0; q < GW_BPL; ++q) {
-        pw[q] = make_float3(pmq[q].x, pmq[q].y, pmq[q].z);
+        float3 p = make_float3(pmq[q].x, pmq[q].y, pmq[q].z);
         if (PREC) {
             const float4 lo_b = b.leaf_lo[actq[q] ? gq[q] : grp.x];
-            pw[q] = make_float3((pmq[q].x - gg.cx) + lo_b.x, (pmq[q].y - gg.cy) + lo_b.y, (pmq[q].z - gg.cz) + lo_b.z);
+            p = make_float3((pmq[q].x - gg.cx) + lo_b.x, (pmq[q].y - gg.cy) + lo_b.y, (pmq[q].z - gg.cz) + lo_b.z);
         }
+        sx(np_, q) = -p.x;
+        sy(np_, q) = -p.y;
+        sz(np_, q) = -p.z;
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
@@ -242,13 +268,16 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         if (lane == 0) S.grp_rad[w] = gr;
         __syncwarp();
     }
-    float ax[GW_BPL], ay[GW_BPL], az[GW_BPL], pot[GW_BPL];
-    float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], np_[GW_BPL];  // PREC: leaf terms (Kahan)
+    Slots3 acc;  // accelerations
+#pragma unroll
+    for (int q = 0; q < GW_BPL; ++q) sx(acc, q) = sy(acc, q) = sz(acc, q) = 0.f;
+    float pot[GW_BPL];
+    float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], npt_[GW_BPL];  // PREC: leaf terms (Kahan)
     float cx_[GW_BPL], cy_[GW_BPL], cz_[GW_BPL], cp_[GW_BPL];
 #pragma unroll
     for (int q = 0; q < GW_BPL; ++q) {
-        ax[q] = ay[q] = az[q] = pot[q] = 0.f;
-        nx_[q] = ny_[q] = nz_[q] = np_[q] = 0.f;
+        pot[q] = 0.f;
+        nx_[q] = ny_[q] = nz_[q] = npt_[q] = 0.f;
         cx_[q] = cy_[q] = cz_[q] = cp_[q] = 0.f;
     }
     uint32_t inter = 0, evals = 0, opened = 0;
@@ -261,6 +290,15 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
     // softening of at least 1e-20 a body's own entry adds exactly zero (its
     // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
     const bool self_check = !(soft >= 1e-20f);
+    // list entry j as (x, y, z, G m)
+    auto list_get = [&](uint32_t j) {
+        const float4 a = lcm[j][0], c = lcm[j][1];
+        return make_float4(a.x, a.z, c.x, c.z);
+    };
+    auto list_put = [&](uint32_t j, float4 c) {
+        lcm[j][0] = make_float4(c.x, c.x, c.y, c.y);
+        lcm[j][1] = make_float4(c.z, c.z, c.w, c.w);
+    };
     // penetration of group body q with the leaf entry j (body id lj, radius
     // kept with the entry): a task when the distance is below the sum of the
     // radii and this body's index is the smaller (bh_force.comp:109-112)
@@ -290,11 +328,11 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             // check, merge tasks
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 c = lcm[j];
+                const float4 c = list_get(j);
                 const uint32_t lj = lid[j];
 #pragma unroll
                 for (int q = 0; q < GW_BPL; ++q) {
-                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                    const float rx = c.x + sx(np_, q), ry = c.y + sy(np_, q), rz = c.z + sz(np_, q);
                     if (merging) merge_test(q, lj, rx, ry, rz, lrad[j]);
                     const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                     const float inv = rsqrtf(rr);
@@ -305,11 +343,11 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                         kahan_add(nx_[q], cx_[q], f * rx);
                         kahan_add(ny_[q], cy_[q], f * ry);
                         kahan_add(nz_[q], cz_[q], f * rz);
-                        if (want_pot) kahan_add(np_[q], cp_[q], ph);
+                        if (want_pot) kahan_add(npt_[q], cp_[q], ph);
                     } else {
-                        ax[q] = __fmaf_rn(f, rx, ax[q]);
-                        ay[q] = __fmaf_rn(f, ry, ay[q]);
-                        az[q] = __fmaf_rn(f, rz, az[q]);
+                        sx(acc, q) = __fmaf_rn(f, rx, sx(acc, q));
+                        sy(acc, q) = __fmaf_rn(f, ry, sy(acc, q));
+                        sz(acc, q) = __fmaf_rn(f, rz, sz(acc, q));
                         if (want_pot) pot[q] += ph;
                     }
                 }
@@ -317,45 +355,55 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         } else if (self_check) {
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 c = lcm[j];
+                const float4 c = list_get(j);
                 const uint32_t lj = lid[j];
 #pragma unroll
                 for (int q = 0; q < GW_BPL; ++q) {
-                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                    const float rx = c.x + sx(np_, q), ry = c.y + sy(np_, q), rz = c.z + sz(np_, q);
                     const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                     const float inv = rsqrtf(rr);
                     const float f = (lj == gq[q]) ? 0.0f : c.w * (inv * inv * inv);
-                    ax[q] = __fmaf_rn(f, rx, ax[q]);
-                    ay[q] = __fmaf_rn(f, ry, ay[q]);
-                    az[q] = __fmaf_rn(f, rz, az[q]);
+                    sx(acc, q) = __fmaf_rn(f, rx, sx(acc, q));
+                    sy(acc, q) = __fmaf_rn(f, ry, sy(acc, q));
+                    sz(acc, q) = __fmaf_rn(f, rz, sz(acc, q));
                 }
             }
         } else {
-            // one loop per number of slots in use (warp-uniform), unrolled
-            // over a constant
-            auto slots = [&](auto qn) {
-                constexpr int Q = decltype(qn)::value;
+            // the hot loop: slots 0 and 1 as one packed FP32x2 pair (every
+            // instruction but the reciprocal square roots serves both), slot
+            // 2 alone when the group has more than 64 bodies (warp-uniform)
+            const float2 s2 = make_float2(soft, soft);
+            auto pairs = [&](auto with_third) {
+                constexpr bool THIRD = decltype(with_third)::value;
 #pragma unroll 2
                 for (uint32_t j = 0; j < cnt; ++j) {
-                    const float4 c = lcm[j];
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) {
-                        const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
-                        const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
-                        const float inv = rsqrtf(rr);
-                        const float f = c.w * (inv * inv * inv);
-                        ax[q] = __fmaf_rn(f, rx, ax[q]);
-                        ay[q] = __fmaf_rn(f, ry, ay[q]);
-                        az[q] = __fmaf_rn(f, rz, az[q]);
+                    const float4 e0 = lcm[j][0], e1 = lcm[j][1];
+                    const float2 cx = make_float2(e0.x, e0.y), cy = make_float2(e0.z, e0.w);
+                    const float2 cz = make_float2(e1.x, e1.y), cw = make_float2(e1.z, e1.w);
+                    const float2 rx = __fadd2_rn(cx, np_.x01), ry = __fadd2_rn(cy, np_.y01), rz = __fadd2_rn(cz, np_.z01);
+                    float2 rr = __ffma2_rn(rx, rx, s2);
+                    rr = __ffma2_rn(ry, ry, rr);
+                    rr = __ffma2_rn(rz, rz, rr);
+                    const float2 inv = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
+                    const float2 f = __fmul2_rn(cw, __fmul2_rn(inv, __fmul2_rn(inv, inv)));
+                    acc.x01 = __ffma2_rn(f, rx, acc.x01);
+                    acc.y01 = __ffma2_rn(f, ry, acc.y01);
+                    acc.z01 = __ffma2_rn(f, rz, acc.z01);
+                    if (THIRD) {
+                        const float tx = e0.x + np_.x2, ty = e0.z + np_.y2, tz = e1.x + np_.z2;
+                        const float t2 = __fmaf_rn(tz, tz, __fmaf_rn(ty, ty, __fmaf_rn(tx, tx, soft)));
+                        const float ti = rsqrtf(t2);
+                        const float tf = e1.z * (ti * (ti * ti));
+                        acc.x2 = __fmaf_rn(tf, tx, acc.x2);
+                        acc.y2 = __fmaf_rn(tf, ty, acc.y2);
+                        acc.z2 = __fmaf_rn(tf, tz, acc.z2);
                     }
                 }
             };
             if (nq >= GW_BPL)
-                slots(std::integral_constant<int, GW_BPL>{});
-            else if (nq == 2)
-                slots(std::integral_constant<int, 2>{});
+                pairs(std::true_type{});
             else
-                slots(std::integral_constant<int, 1>{});
+                pairs(std::false_type{});
         }
         if (merging && !(PREC || want_pot)) {
             // merge tests outside the force loop: lane j screens entry j with
@@ -367,7 +415,7 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
                 bool near = false;
                 if (j0 + lane < cnt && lid[j0 + lane] < N) {
-                    const float4 c = lcm[j0 + lane];
+                    const float4 c = list_get(j0 + lane);
                     const float dx = fmaxf(fmaxf(bmn.x - c.x, c.x - bmx.x), 0.0f);
                     const float dy = fmaxf(fmaxf(bmn.y - c.y, c.y - bmx.y), 0.0f);
                     const float dz = fmaxf(fmaxf(bmn.z - c.z, c.z - bmx.z), 0.0f);
@@ -378,12 +426,12 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
                 while (m) {
                     const uint32_t j = j0 + __ffs(m) - 1;
                     m &= m - 1;
-                    const float4 c = lcm[j];
+                    const float4 c = list_get(j);
                     const uint32_t lj = lid[j];
                     const float lr = lrad[j];
 #pragma unroll
                     for (int q = 0; q < GW_BPL; ++q)
-                        merge_test(q, lj, c.x - pw[q].x, c.y - pw[q].y, c.z - pw[q].z, lr);
+                        merge_test(q, lj, c.x + sx(np_, q), c.y + sy(np_, q), c.z + sz(np_, q), lr);
                 }
             }
         }
@@ -402,9 +450,9 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         if (kind == 1) {
             const uint32_t pos = ln + __popc(bl & lanemask_lt());
             if (PREC)
-                lcm[pos] = make_float4((cm.x - gg.cx) + lo.x, (cm.y - gg.cy) + lo.y, (cm.z - gg.cz) + lo.z, G * cm.w);
+                list_put(pos, make_float4((cm.x - gg.cx) + lo.x, (cm.y - gg.cy) + lo.y, (cm.z - gg.cz) + lo.z, G * cm.w));
             else
-                lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
+                list_put(pos, make_float4(cm.x, cm.y, cm.z, G * cm.w));
             lid[pos] = id;
             if (merging) lrad[pos] = lo.x;  // the leaf's radius, read at the pop (0 for nodes)
         }
@@ -422,7 +470,8 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
             ln -= 32;
             __syncwarp();
             if (lane < ln) {  // move the remaining entries to the front
-                lcm[lane] = lcm[32 + lane];
+                lcm[lane][0] = lcm[32 + lane][0];
+                lcm[lane][1] = lcm[32 + lane][1];
                 lid[lane] = lid[32 + lane];
                 if (merging) lrad[lane] = lrad[32 + lane];
             }
@@ -571,12 +620,12 @@ __global__ __launch_bounds__(GW_THREADS, (MODE == GM_THETA && FORM == FORM_FP32)
         // body index and position again (not kept live through the walk)
         const uint32_t bi = b.idx_in[gq[q]];
         const float4 pm = b.leaf_pm[gq[q]];
-        float fx = ax[q], fy = ay[q], fz = az[q], fp = pot[q];
+        float fx = sx(acc, q), fy = sy(acc, q), fz = sz(acc, q), fp = pot[q];
         if (PREC) {
             fx = fx + (nx_[q] - cx_[q]);
             fy = fy + (ny_[q] - cy_[q]);
             fz = fz + (nz_[q] - cz_[q]);
-            fp = fp + (np_[q] - cp_[q]);
+            fp = fp + (npt_[q] - cp_[q]);
         }
         if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(fx, fy, fz, 0.0f);
         if (b.accel_mag) b.accel_mag[bi] = sqrtf(fx * fx + fy * fy + fz * fz);
