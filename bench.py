@@ -340,6 +340,46 @@ def precision_arm(bh, p_plain, accuracy):
     return p64, calib
 
 
+def train_out_of_sample(bh, args, local) -> dict:
+    """The learned criterion's weights from training pairs recorded on
+    snapshots of two other workloads, the two-galaxy encounter (8,388,608
+    bodies) and the uniform cube with merges (1,048,576 bodies), one step into
+    each run; the timed state is never seen in training.  Recording and
+    training are deterministic, so every run trains the same weights."""
+    from gravity_gb300 import BarnesHut
+
+    t0 = time.perf_counter()
+    feats, labels, sources = [], [], []
+    for name, share in (("galaxy", 0.75), ("uniform_merge", 0.25)):
+        wl = workload(name, None)
+        b = wl["bodies"]()
+        bounds = wl.get("bounds", ic.exact_bounds(b))
+        p = abi.StepParams.from_buffer_copy(wl["params"])
+        p.merging_collision_or_neither = abi.MODE_NEITHER  # the field only
+        p.precision_mode = abi.PRECISION_FP32
+        sim = BarnesHut(wl["n"], bounds, abi.units(G=1.0), device=local)
+        sim.upload_bodies(b)
+        sim.init()
+        sim.step(p)
+        k = sim.mac_generate(p, max_pairs=int(args.mac_pairs * share), seed=1)
+        f, lab = sim.mac_read_pairs(k)
+        feats.append(f)
+        labels.append(lab)
+        sources.append({"workload": wl["name"], "pairs": int(k)})
+        sim.close()
+    F = np.concatenate(feats)
+    L = np.concatenate(labels)
+    t1 = time.perf_counter()
+    bh.mac_write_pairs(F, L)
+    losses = bh.mac_train(epochs=args.mac_epochs, batch=16384, lr=3e-3, seed=0)
+    w = bh.mac_get_weights()
+    if args.save_mac_weights:
+        np.save(args.save_mac_weights, w)
+    return {"sources": sources, "pairs": int(len(L)), "epochs": args.mac_epochs, "loss_first": float(losses[0]),
+            "loss_last": float(losses[-1]), "record_s": t1 - t0, "train_s": time.perf_counter() - t1,
+            "weights_sha256": __import__("hashlib").sha256(w.tobytes()).hexdigest()[:16]}
+
+
 def kernels_per_step(mac_mode: int) -> int:
     """Kernels of this library launched by one step (the CUDA graph's kernel
     nodes): reset 1, prepare 3, sort 1 + 8 passes, build 1, fill 2, walk 1
@@ -396,13 +436,18 @@ def run_ours(args):
         if args.mac_weights:
             bh.mac_set_weights(np.load(args.mac_weights))
             calib["weights"] = os.path.basename(args.mac_weights)
-        else:
+            calib["weights_source"] = "loaded: " + os.path.basename(args.mac_weights)
+        elif args.train_in_sample:
             p_grav = abi.StepParams.from_buffer_copy(p_plain)
             p_grav.merging_collision_or_neither = abi.MODE_NEITHER  # the field only
             pairs = bh.mac_generate(p_grav, max_pairs=args.mac_pairs, seed=1)
             losses = bh.mac_train(epochs=args.mac_epochs, batch=16384, lr=3e-3, seed=0)
             calib["training"] = {"pairs": pairs, "epochs": args.mac_epochs, "loss_first": float(losses[0]),
                                  "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
+            calib["weights_source"] = "in-sample: trained on the timed state"
+        else:
+            calib["training"] = train_out_of_sample(bh, args, local)
+            calib["weights_source"] = "out-of-sample: galaxy-pair and uniform-cube snapshots"
         ref_sample = accuracy.DirectSumSample(bh, p_plain, count=4096, seed=2)
         calib["judge"] = ref_sample.judge
         ref = {th: accuracy.evaluate(bh, ref_sample, plain(th)) for th in PLAIN_THETAS}
@@ -501,22 +546,32 @@ def run_ours(args):
         traffic = WALK_LEARNED_DRAM_BYTES_PER_BODY * n_live
 
     # ---- e2e through the public API with host buffers: every step's bodies go
-    # host->device from pinned memory and its result comes back.  Between two
-    # steps one gbh_exchange_bodies call reads the last result while it
-    # writes the next input (the copies overlap chunk by chunk); the first
-    # input and the last result are copied alone.
+    # host->device from pinned memory and its result (all bodies) comes back.
+    # Headline form (streamed): each gbh_step_streamed call runs one step while
+    # the next step's input goes up and the previous step's result comes down
+    # on the copy engines; the first input is uploaded before the first call
+    # and the last result read by gbh_step_streamed_finish, both inside the
+    # timed region.  Also measured: the exchange form (read-back and next
+    # upload overlapped with each other, between steps) and the serial form.
     n = wl["n"]
     pin_in = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
     pin_out = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
     bh.read_bodies(out=pin_in)
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 20))
     bh.step(p_head)  # warm the graph of this parity
     bh.read_bodies(out=pin_in)
+    bh.step_streamed(p_head, None, None)  # allocates the staging buffers
+    bh.step_streamed_finish(None)
 
-    def e2e_run(overlap):
+    def e2e_run(form):
         barrier(dist, local)
         t0 = time.perf_counter()
-        if overlap:
+        if form == "streamed":
+            bh.upload_bodies(pin_in, chunk=n)
+            for k in range(e2e_steps):
+                bh.step_streamed(p_head, pin_in if k + 1 < e2e_steps else None, pin_out if k else None)
+            bh.step_streamed_finish(pin_out)
+        elif form == "exchange":
             bh.upload_bodies(pin_in, chunk=n)
             bh.step(p_head)
             for _ in range(e2e_steps - 1):
@@ -530,15 +585,21 @@ def run_ours(args):
                 bh.read_bodies(out=pin_out)
         return max_over_ranks(dist, time.perf_counter() - t0, local)
 
-    e2e_serial_s = e2e_run(False)
-    e2e_s = e2e_run(True)
+    e2e_serial_s = e2e_run("serial")
+    e2e_exchange_s = e2e_run("exchange")
+    e2e_s = e2e_run("streamed")
     e2e = {
         "value": world * e2e_steps / e2e_s,
         "unit": "steps/s",
         "h2d_bytes_per_step": n * abi.BODY_DTYPE.itemsize + C.sizeof(abi.StepParams),
         "d2h_bytes_per_step": n * abi.BODY_DTYPE.itemsize,
-        "path": "BarnesHut.upload_bodies + step, then per step exchange_bodies + step, then read_bodies "
-                "(C-ABI gbh_upload_bodies / gbh_step / gbh_exchange_bodies / gbh_read_bodies), pinned host buffers",
+        "steps": e2e_steps,
+        "path": "BarnesHut.upload_bodies, then per step step_streamed (C-ABI gbh_step_streamed: the step, the next "
+                "input's upload and the previous result's read-back overlapped), then step_streamed_finish; "
+                "pinned host buffers, every step's whole state up and its whole result down",
+        "exchange_value": world * e2e_steps / e2e_exchange_s,
+        "exchange_path": "per step gbh_exchange_bodies (read-back and next upload overlapped with each other) + "
+                         "gbh_step",
         "serial_value": world * e2e_steps / e2e_serial_s,
         "serial_path": "per step upload_bodies + step + read_bodies, one copy direction at a time",
     }
@@ -643,7 +704,11 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip the plain and group-theta comparison arms")
     ap.add_argument("--mac-weights", default=None, help="load MLP weights (.npy) instead of training")
     ap.add_argument("--mac-tolerance", type=float, default=None, help="fixed tolerance instead of calibration")
-    ap.add_argument("--mac-pairs", type=int, default=8_000_000)
+    ap.add_argument("--mac-pairs", type=int, default=48_000_000,
+                    help="training pairs (split 3:1 between the galaxy-pair and uniform-cube snapshots)")
+    ap.add_argument("--train-in-sample", action="store_true",
+                    help="record the training pairs on the timed state itself (default: other workloads)")
+    ap.add_argument("--save-mac-weights", default=None, help="save the trained MLP weights (.npy)")
     ap.add_argument("--mac-epochs", type=int, default=12)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

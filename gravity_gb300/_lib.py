@@ -73,6 +73,8 @@ def _declare(L):
         "gbh_mac_predict": [vp, vp, u32, vp],
         "gbh_sort_pairs_noalloc": [vp, vp, vp, vp, u32, vp],
         "gbh_exchange_bodies": [vp, vp, vp, u32, u32],
+        "gbh_step_streamed": [vp, sp, vp, vp],
+        "gbh_step_streamed_finish": [vp, vp],
         "gbh_generate_bodies": [vp, C.POINTER(abi.IcParams), u64, u32, u32],
         "gbh_select_glow_nodes": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],
         "gbh_select_regions": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],

@@ -79,6 +79,29 @@ class BarnesHut:
         self._chk(lib().gbh_exchange_bodies(self._h, _ptr(out), _ptr(b), len(b), offset))
         return out
 
+    def _whole_state(self, a: np.ndarray | None, what: str, writable: bool):
+        if a is None:
+            return None
+        if a.dtype != abi.BODY_DTYPE or len(a) != self.n or not a.flags.c_contiguous or (writable and not a.flags.writeable):
+            raise ValueError(f"{what} must be a contiguous BODY_DTYPE array of initial_num_bodies bodies")
+        return a
+
+    def step_streamed(self, params: abi.StepParams, next_input: np.ndarray | None, last_result: np.ndarray | None):
+        """One step on the current state; while it runs, `next_input` goes to
+        the device (it becomes the state after this step) and the previous
+        call's result comes back into `last_result` (gbh_step_streamed)."""
+        nxt = self._whole_state(next_input, "next_input", False)
+        out = self._whole_state(last_result, "last_result", True)
+        self._chk(lib().gbh_step_streamed(self._h, C.byref(params), None if nxt is None else _ptr(nxt),
+                                          None if out is None else _ptr(out)))
+        return last_result
+
+    def step_streamed_finish(self, last_result: np.ndarray | None):
+        """The last streamed step's result (gbh_step_streamed_finish)."""
+        out = self._whole_state(last_result, "last_result", True)
+        self._chk(lib().gbh_step_streamed_finish(self._h, None if out is None else _ptr(out)))
+        return last_result
+
     def generate_bodies(self, params: abi.IcParams, seed: int = 0, count: int | None = None, offset: int = 0):
         """Seeded initial conditions written on the device (gbh_generate_bodies)."""
         count = self.n - offset if count is None else count

@@ -60,6 +60,7 @@ struct DevState {
     uint32_t merge_tasks;
     uint32_t sort_tiles[SORT_PASSES];  // onesweep tile tickets
     uint32_t num_groups;               // body groups of the group walk
+    uint32_t group_next;               // the next group a warp of the group walk takes (ticket)
     uint32_t frontier_saturated;       // group walks that accepted instead of opening (full stack)
     uint32_t fill_frontier;            // nodes handed from the tiled fill to the top-tree fill
     uint32_t sorted_valid;             // sorted_pm holds the current positions in index order
@@ -303,6 +304,10 @@ __device__ __forceinline__ void kahan_add(float& sum, float& c, float x) {
 void launch_reset(const StepBuffers& b, cudaStream_t s);
 void launch_prepare(const StepBuffers& b, cudaStream_t s);
 void launch_sort(const StepBuffers& b, cudaStream_t s);
+// histograms for launch_sort when the keys come from elsewhere than the encode
+// pass (hist must be zero; also sets st->n_new = n)
+void launch_sort_hist(const uint64_t* keys, uint32_t n, uint32_t* hist, DevState* st, uint32_t num_sms,
+                      cudaStream_t s);
 void launch_generate_bodies(gbh_body* bodies, uint32_t count, uint32_t offset, const gbh_ic_params& p, uint64_t seed,
                             cudaStream_t s);
 void launch_build(const StepBuffers& b, cudaStream_t s);

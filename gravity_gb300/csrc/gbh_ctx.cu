@@ -388,6 +388,14 @@ int gbh_destroy(gbh_ctx* c) {
             if (e) cudaEventDestroy(e);
         cudaStreamDestroy(c->copy_stream);
     }
+    if (c->copy_stream2) {
+        cudaStreamSynchronize(c->copy_stream2);
+        cudaStreamDestroy(c->copy_stream2);
+    }
+    for (cudaEvent_t e : {c->ev_in_ready, c->ev_in_free, c->ev_out_ready, c->ev_out_done})
+        if (e) cudaEventDestroy(e);
+    cudaFree(c->stage_in);
+    cudaFree(c->stage_out);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return GBH_OK;
@@ -434,6 +442,75 @@ int gbh_exchange_bodies(gbh_ctx* c, gbh_body* host_out, const gbh_body* host_in,
     CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     return GBH_OK;
+}
+
+// Staging buffers, the second copy stream and the events of the streamed
+// steps, created on first use (two body buffers: 64 bytes per body).
+static int ensure_stream_buffers(gbh_ctx* c) {
+    if (c->stage_in) return GBH_OK;
+    const size_t bytes = (size_t)c->N * sizeof(gbh_body);
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy_stream2, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c->ev_in_ready, &c->ev_in_free, &c->ev_out_ready, &c->ev_out_done})
+        CUDA_TRY(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    CUDA_TRY(c, cudaMalloc(&c->stage_out, bytes));
+    CUDA_TRY(c, cudaMalloc(&c->stage_in, bytes));
+    return GBH_OK;
+}
+
+int gbh_step_streamed(gbh_ctx* c, const gbh_step_params* p, const gbh_body* next_input, gbh_body* last_result) {
+    if (!c) return GBH_ERR_INVALID;
+    if (!c->inited) return fail(c, GBH_ERR_STATE, "gbh_step_streamed before gbh_init");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = ensure_stream_buffers(c);
+    if (rc) return rc;
+    const size_t bytes = (size_t)c->N * sizeof(gbh_body);
+    // the last call's result out of stage_out, once it is there
+    const bool give = c->stream_have_result && last_result;
+    if (give) {
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream2, c->ev_out_ready, 0));
+        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->stage_out, bytes, cudaMemcpyDeviceToHost, c->copy_stream2));
+    }
+    CUDA_TRY(c, cudaEventRecord(c->ev_out_done, c->copy_stream2));
+    // the next input into stage_in, once the last one has left it
+    if (next_input) {
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_in_free, 0));
+        CUDA_TRY(c, cudaMemcpyAsync(c->stage_in, next_input, bytes, cudaMemcpyHostToDevice, c->copy_stream));
+        CUDA_TRY(c, cudaEventRecord(c->ev_in_ready, c->copy_stream));
+    }
+    // this call's step on the current state (one graph launch)
+    if ((rc = gbh_step_n(c, p, 1))) return rc;
+    // its result into stage_out once the read-back above has finished with it
+    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_out_done, 0));
+    CUDA_TRY(c, cudaMemcpyAsync(c->stage_out, c->bodies[c->bin], bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CUDA_TRY(c, cudaEventRecord(c->ev_out_ready, c->stream));
+    c->stream_have_result = true;
+    if (next_input) {
+        // the next input becomes the current state
+        CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_in_ready, 0));
+        CUDA_TRY(c, cudaMemcpyAsync(c->bodies[c->bin], c->stage_in, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, cudaEventRecord(c->ev_in_free, c->stream));
+        c->pos64_valid = false;
+        ++c->state_epoch;
+        if ((rc = invalidate_sorted(c))) return rc;
+    }
+    // the host buffers are free again; the step itself may still run
+    CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream2));
+    return GBH_OK;
+}
+
+int gbh_step_streamed_finish(gbh_ctx* c, gbh_body* last_result) {
+    if (!c) return GBH_ERR_INVALID;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!c->stream_have_result) return fail(c, GBH_ERR_STATE, "no streamed step has run since the last finish");
+    if (last_result) {
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream2, c->ev_out_ready, 0));
+        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->stage_out, (size_t)c->N * sizeof(gbh_body),
+                                    cudaMemcpyDeviceToHost, c->copy_stream2));
+        CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream2));
+    }
+    c->stream_have_result = false;
+    return gbh_synchronize(c);
 }
 
 int gbh_generate_bodies(gbh_ctx* c, const gbh_ic_params* p, uint64_t seed, uint32_t count, uint32_t offset) {

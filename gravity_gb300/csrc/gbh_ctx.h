@@ -76,6 +76,15 @@ struct gbh_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_events[16] = {};
 
+    // gbh_step_streamed: the next input and the last result in device
+    // staging buffers (allocated on first use), the read-back on a second
+    // copy stream, and the events that order the copies with the steps
+    gbh_body* stage_in = nullptr;
+    gbh_body* stage_out = nullptr;
+    cudaStream_t copy_stream2 = nullptr;
+    cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_done = nullptr;
+    bool stream_have_result = false;  // stage_out holds the result of the last streamed step
+
     std::map<int, cudaGraphExec_t> graphs;
     std::string last_error;
 };

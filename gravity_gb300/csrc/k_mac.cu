@@ -13,14 +13,21 @@
 //      |a_i|; the label is log10 of the maximum over the group.  Subtrees of
 //      at most 1024 bodies are summed exactly over their contiguous sorted
 //      leaf range; larger ones by a strict walk of the subtree.
+//   Which pairs are kept depends only on (group, node): the group is named by
+//   its first sorted slot, and a pass that would overflow the budget is run
+//   again with a smaller keep fraction.  The kept pairs are then sorted by
+//   (group, node) with the step's radix sort, so that the pair list, and
+//   with it every minibatch, is the same in every run.
 // Training (gbh_mac_train): minibatches drawn with a counter-based hash; the
 // forward pass is the inference code (BF16 mma.sync, FP32 accumulation), the
 // backward pass runs in FP32 on the CUDA cores (straight-through for the BF16
-// rounding), gradients reduce per warp and add atomically, then Adam updates
+// rounding), each warp writes its gradient sums, one kernel adds them in warp
+// order (no float atomics: training is bit-reproducible), then Adam updates
 // the FP32 master weights and rebuilds the BF16 fragment table.
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "gbh_ctx.h"
@@ -55,7 +62,24 @@ struct MacState {
     uint32_t cap = 0;
     uint32_t num_pairs = 0;
     uint64_t adam_t = 0;
+    // sorting the recorded pairs by (group, node): keys and row indices
+    // (ping-pong), the sort's histograms, look-back words and counters, and
+    // the gathered copies of the pairs and features
+    uint64_t* skeys[2] = {nullptr, nullptr};
+    uint32_t* svals[2] = {nullptr, nullptr};
+    uint32_t* shist = nullptr;
+    uint32_t* sbase = nullptr;
+    uint32_t* slook = nullptr;
+    DevState* sst = nullptr;
+    uint32_t stiles = 0;
+    float* feats_tmp = nullptr;
+    uint2* pairs_tmp = nullptr;
+    // per-warp gradient sums of one training step [warps][MAC_NPARAMS + 1]
+    float* part = nullptr;
+    uint32_t part_warps = 0;
 };
+
+#define MAC_PART_STRIDE (MAC_NPARAMS + 1)  // the parameters' gradients, then the loss
 
 // ---------------------------------------------------------------------------
 // fragment table from the FP32 parameters (layout in mac_mlp.cuh)
@@ -206,6 +230,28 @@ __global__ void k_mac_label(StepBuffers b, const uint2* __restrict__ pairs, cons
 }
 
 // ---------------------------------------------------------------------------
+// canonical order of the recorded pairs: key (group's first sorted slot, node)
+__global__ void k_mac_pair_keys(const uint2* __restrict__ pairs, const uint2* __restrict__ groups, uint32_t n,
+                                uint64_t* __restrict__ keys, uint32_t* __restrict__ rows) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint2 pr = pairs[p];
+    keys[p] = ((uint64_t)groups[pr.x].x << 32) | pr.y;
+    rows[p] = p;
+}
+
+__global__ void k_mac_gather_pairs(const uint32_t* __restrict__ rows, uint32_t n, const float* __restrict__ feats,
+                                   const uint2* __restrict__ pairs, float* __restrict__ feats_out,
+                                   uint2* __restrict__ pairs_out) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const uint32_t src = rows[r];
+#pragma unroll
+    for (int k = 0; k < MAC_FEATURES; ++k) feats_out[(size_t)r * MAC_FEATURES + k] = feats[(size_t)src * MAC_FEATURES + k];
+    pairs_out[r] = pairs[src];
+}
+
+// ---------------------------------------------------------------------------
 // training: forward (tensor cores) + backward (FP32) of 32 samples per warp
 struct TrainSmem {
     alignas(16) uint32_t frag[MAC_SMEM_FRAG_WORDS];
@@ -225,7 +271,7 @@ __device__ __forceinline__ uint32_t sample_index(uint32_t seed, uint32_t step, u
 __global__ __launch_bounds__(MAC_TRAIN_WARPS * 32) void k_mac_train_step(
     const float* __restrict__ feats, const float* __restrict__ labels, uint32_t n_pairs, uint32_t total,
     int random, uint32_t seed, uint32_t step, MacDeviceWeights mw, const float* __restrict__ params,
-    float* __restrict__ grad, float* __restrict__ loss) {
+    float* __restrict__ part) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     mac_load_frag(mw, S.frag, S.x);
@@ -296,19 +342,35 @@ __global__ __launch_bounds__(MAC_TRAIN_WARPS * 32) void k_mac_train_step(
 #pragma unroll
         for (int k = 0; k < MAC_FEATURES; ++k) g_w1[k] = fmaf(z1, __bfloat162float(X[s * 16 + k]), g_w1[k]);
     }
+    // this warp's sums: every parameter once (lane o: the weights of unit o)
+    float* gp = part + (size_t)(blockIdx.x * MAC_TRAIN_WARPS + w) * MAC_PART_STRIDE;
 #pragma unroll
-    for (int k = 0; k < MAC_FEATURES; ++k) atomicAdd(&grad[MAC_OFF_W1 + o * MAC_FEATURES + k], g_w1[k]);
-    atomicAdd(&grad[MAC_OFF_B1 + o], g_b1);
+    for (int k = 0; k < MAC_FEATURES; ++k) gp[MAC_OFF_W1 + o * MAC_FEATURES + k] = g_w1[k];
+    gp[MAC_OFF_B1 + o] = g_b1;
 #pragma unroll
-    for (int k = 0; k < 32; ++k) atomicAdd(&grad[MAC_OFF_W2 + o * 32 + k], g_w2[k]);
-    atomicAdd(&grad[MAC_OFF_B2 + o], g_b2);
-    atomicAdd(&grad[MAC_OFF_W3 + o], g_w3);
+    for (int k = 0; k < 32; ++k) gp[MAC_OFF_W2 + o * 32 + k] = g_w2[k];
+    gp[MAC_OFF_B2 + o] = g_b2;
+    gp[MAC_OFF_W3 + o] = g_w3;
 #pragma unroll
     for (int s = 16; s > 0; s >>= 1) l += __shfl_xor_sync(0xffffffffu, l, s);
     if (lane == 0) {
-        atomicAdd(&grad[MAC_OFF_B3], g_b3);
-        atomicAdd(&loss[0], l);
+        gp[MAC_OFF_B3] = g_b3;
+        gp[MAC_NPARAMS] = l;
     }
+}
+
+// The gradient of one step: the warps' sums added in warp order (the same
+// bits in every run); the loss slot adds into the epoch's running loss.
+__global__ void k_mac_reduce(const float* __restrict__ part, uint32_t warps, float* __restrict__ grad,
+                             float* __restrict__ loss) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > MAC_NPARAMS) return;
+    float sum = 0.0f;
+    for (uint32_t w = 0; w < warps; ++w) sum += part[(size_t)w * MAC_PART_STRIDE + i];
+    if (i < MAC_NPARAMS)
+        grad[i] = sum;
+    else
+        loss[0] += sum;
 }
 
 __global__ void k_mac_adam(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
@@ -358,20 +420,84 @@ static int mac_ensure(gbh_ctx* c) {
     return GBH_OK;
 }
 
+static void mac_free_pairs(MacState* m) {
+    for (void* p : {(void*)m->feats, (void*)m->labels, (void*)m->pairs, (void*)m->skeys[0], (void*)m->skeys[1],
+                    (void*)m->svals[0], (void*)m->svals[1], (void*)m->shist, (void*)m->sbase, (void*)m->slook,
+                    (void*)m->sst, (void*)m->feats_tmp, (void*)m->pairs_tmp})
+        cudaFree(p);
+    m->feats = m->feats_tmp = nullptr;
+    m->labels = nullptr;
+    m->pairs = m->pairs_tmp = nullptr;
+    m->skeys[0] = m->skeys[1] = nullptr;
+    m->svals[0] = m->svals[1] = nullptr;
+    m->shist = m->sbase = m->slook = nullptr;
+    m->sst = nullptr;
+    m->cap = 0;
+}
+
+// pair buffers for `cap` pairs, with the buffers of their canonical sort
 static int mac_ensure_pairs(gbh_ctx* c, uint32_t cap) {
     MacState* m = c->mac;
     if (m->cap >= cap) return GBH_OK;
-    cudaFree(m->feats);
-    cudaFree(m->labels);
-    cudaFree(m->pairs);
-    m->feats = nullptr;
-    m->labels = nullptr;
-    m->pairs = nullptr;
-    m->cap = 0;
+    mac_free_pairs(m);
+    const uint32_t tiles = (cap + SORT_TILE - 1) / SORT_TILE;
     MTRY(c, cudaMalloc(&m->feats, (size_t)cap * MAC_FEATURES * 4));
     MTRY(c, cudaMalloc(&m->labels, (size_t)cap * 4));
     MTRY(c, cudaMalloc(&m->pairs, (size_t)cap * 8));
+    MTRY(c, cudaMalloc(&m->feats_tmp, (size_t)cap * MAC_FEATURES * 4));
+    MTRY(c, cudaMalloc(&m->pairs_tmp, (size_t)cap * 8));
+    for (int k = 0; k < 2; ++k) {
+        MTRY(c, cudaMalloc(&m->skeys[k], (size_t)cap * 8));
+        MTRY(c, cudaMalloc(&m->svals[k], (size_t)cap * 4));
+    }
+    MTRY(c, cudaMalloc(&m->shist, SORT_PASSES * SORT_RADIX * 4));
+    MTRY(c, cudaMalloc(&m->sbase, SORT_PASSES * SORT_RADIX * 4));
+    MTRY(c, cudaMalloc(&m->slook, (size_t)SORT_PASSES * tiles * SORT_RADIX * 4));
+    MTRY(c, cudaMalloc(&m->sst, sizeof(DevState)));
+    m->stiles = tiles;
     m->cap = cap;
+    return GBH_OK;
+}
+
+// Sort the n recorded pairs (and their features) by (group's first sorted
+// slot, node): the step's onesweep radix sort on the 64-bit keys, then one
+// gather.  Needs the groups of the recording walks in c->groups.
+static int mac_sort_pairs(gbh_ctx* c, uint32_t n) {
+    MacState* m = c->mac;
+    if (n < 2) return GBH_OK;
+    const uint32_t threads = 256, blocks = (n + threads - 1) / threads;
+    k_mac_pair_keys<<<blocks, threads, 0, c->stream>>>(m->pairs, c->groups, n, m->skeys[0], m->svals[0]);
+    MTRY(c, cudaGetLastError());
+    const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    MTRY(c, cudaMemsetAsync(m->shist, 0, SORT_PASSES * SORT_RADIX * 4, c->stream));
+    MTRY(c, cudaMemsetAsync(m->sst, 0, sizeof(DevState), c->stream));
+    for (uint32_t p = 0; p < SORT_PASSES; ++p)
+        MTRY(c, cudaMemsetAsync(m->slook + (size_t)p * m->stiles * SORT_RADIX, 0, (size_t)tiles * SORT_RADIX * 4,
+                                c->stream));
+    launch_sort_hist(m->skeys[0], n, m->shist, m->sst, c->num_sms, c->stream);
+    StepBuffers sb;
+    memset(&sb, 0, sizeof(sb));
+    sb.keys_in = m->skeys[0];
+    sb.idx_in = m->svals[0];
+    sb.keys_out = m->skeys[1];
+    sb.idx_out = m->svals[1];
+    sb.st = m->sst;
+    sb.hist = m->shist;
+    sb.bucket_base = m->sbase;
+    sb.lookback = m->slook;
+    sb.N = n;
+    sb.sort_tiles_cap = m->stiles;
+    sb.num_sms = c->num_sms;
+    launch_sort(sb, c->stream);  // eight passes: the result is back in skeys[0], svals[0]
+    k_mac_gather_pairs<<<blocks, threads, 0, c->stream>>>(m->svals[0], n, m->feats, m->pairs, m->feats_tmp,
+                                                           m->pairs_tmp);
+    MTRY(c, cudaGetLastError());
+    uint32_t err = 0;
+    MTRY(c, cudaMemcpyAsync(&err, &m->sst->error_word, 4, cudaMemcpyDeviceToHost, c->stream));
+    MTRY(c, cudaStreamSynchronize(c->stream));
+    if (err) return mac_fail(c, GBH_ERR_DEVICE, "sorting the training pairs: device error word set");
+    std::swap(m->feats, m->feats_tmp);
+    std::swap(m->pairs, m->pairs_tmp);
     return GBH_OK;
 }
 
@@ -386,9 +512,8 @@ void mac_release(gbh_ctx* c) {
     cudaFree(m->loss);
     cudaFree(m->count);
     cudaFree(m->band);
-    cudaFree(m->feats);
-    cudaFree(m->labels);
-    cudaFree(m->pairs);
+    cudaFree(m->part);
+    mac_free_pairs(m);
     delete m;
     c->mac = nullptr;
 }
@@ -542,16 +667,23 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
         MTRY(c, cudaGetLastError());
         MTRY(c, cudaMemcpyAsync(&met, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
         MTRY(c, cudaStreamSynchronize(c->stream));
-        const double frac = met ? 0.95 * (double)budget / (16.0 * (double)met) : 1.0;
-        mw.rec_keep = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
-        // record pass, appending after the pairs kept so far
-        MTRY(c, cudaMemcpyAsync(m->count, &start, 4, cudaMemcpyHostToDevice, c->stream));
-        mw.rec_cap = cap;
-        launch_walk_group_record(ctx_buffers(c), mw, c->stream);
-        MTRY(c, cudaGetLastError());
+        double frac = met ? 0.95 * (double)budget / (16.0 * (double)met) : 1.0;
+        // record pass, appending after the pairs kept so far; a pass that
+        // meets more kept pairs than the budget holds (the ones stored would
+        // then depend on the order the warps ran in) runs again with a
+        // smaller fraction
         uint32_t end = 0;
-        MTRY(c, cudaMemcpyAsync(&end, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
-        MTRY(c, cudaStreamSynchronize(c->stream));
+        for (int attempt = 0;; ++attempt) {
+            mw.rec_keep = frac >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(frac * 4294967296.0);
+            MTRY(c, cudaMemcpyAsync(m->count, &start, 4, cudaMemcpyHostToDevice, c->stream));
+            mw.rec_cap = cap;
+            launch_walk_group_record(ctx_buffers(c), mw, c->stream);
+            MTRY(c, cudaGetLastError());
+            MTRY(c, cudaMemcpyAsync(&end, m->count, 4, cudaMemcpyDeviceToHost, c->stream));
+            MTRY(c, cudaStreamSynchronize(c->stream));
+            if (end <= cap || attempt == 8) break;
+            frac *= 0.95 * (double)budget / (double)(end - start);
+        }
         start = end < cap ? end : cap;
         MTRY(c, cudaMemcpyAsync(m->count, &start, 4, cudaMemcpyHostToDevice, c->stream));
     }
@@ -560,6 +692,8 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
     MTRY(c, cudaStreamSynchronize(c->stream));
     recorded = recorded < max_pairs ? recorded : max_pairs;
     MTRY(c, cudaMemcpyAsync(m->count, &recorded, 4, cudaMemcpyHostToDevice, c->stream));
+    // canonical order of the pairs (and so of every minibatch)
+    if ((rc = mac_sort_pairs(c, recorded))) return rc;
     // 3. labels
     if (recorded) {
         const uint32_t threads = 256;
@@ -664,13 +798,21 @@ int gbh_mac_train(gbh_ctx* c, uint32_t epochs, uint32_t batch, float lr, uint64_
     MTRY(c, cudaFuncSetAttribute(k_mac_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
     const uint32_t rows = MAC_TRAIN_WARPS * 32;
     const uint32_t steps = (m->num_pairs + batch - 1) / batch;
+    const uint32_t tblocks = (batch + rows - 1) / rows, warps = tblocks * MAC_TRAIN_WARPS;
+    if (m->part_warps < warps) {
+        cudaFree(m->part);
+        m->part = nullptr;
+        m->part_warps = 0;
+        MTRY(c, cudaMalloc(&m->part, (size_t)warps * MAC_PART_STRIDE * 4));
+        m->part_warps = warps;
+    }
     for (uint32_t ep = 0; ep < epochs; ++ep) {
         MTRY(c, cudaMemsetAsync(m->loss, 0, 16, c->stream));
         for (uint32_t s = 0; s < steps; ++s) {
             const uint32_t st = ep * steps + s;
-            k_mac_train_step<<<(batch + rows - 1) / rows, rows, train_smem(), c->stream>>>(
-                m->feats, m->labels, m->num_pairs, batch, 1, (uint32_t)seed, st, mac_weights(c), m->params, m->grad,
-                m->loss);
+            k_mac_train_step<<<tblocks, rows, train_smem(), c->stream>>>(
+                m->feats, m->labels, m->num_pairs, batch, 1, (uint32_t)seed, st, mac_weights(c), m->params, m->part);
+            k_mac_reduce<<<(MAC_PART_STRIDE + 255) / 256, 256, 0, c->stream>>>(m->part, warps, m->grad, m->loss);
             ++m->adam_t;
             const float bc1 = 1.0f - std::pow(0.9f, (float)m->adam_t);
             const float bc2 = 1.0f - std::pow(0.999f, (float)m->adam_t);
@@ -696,9 +838,12 @@ int gbh_mac_loss_grad(gbh_ctx* c, const float* features, const float* labels, ui
     if (!c->mac_ready) return mac_fail(c, GBH_ERR_STATE, "no weights");
     MTRY(c, cudaSetDevice(c->device));
     MacState* m = c->mac;
-    float *df = nullptr, *dl = nullptr;
+    float *df = nullptr, *dl = nullptr, *dp = nullptr;
+    const uint32_t rows = MAC_TRAIN_WARPS * 32, tblocks = (count + rows - 1) / rows;
+    const uint32_t warps = tblocks * MAC_TRAIN_WARPS;
     MTRY(c, cudaMalloc(&df, (size_t)count * MAC_FEATURES * 4));
     MTRY(c, cudaMalloc(&dl, (size_t)count * 4));
+    MTRY(c, cudaMalloc(&dp, (size_t)warps * MAC_PART_STRIDE * 4));
     cudaError_t e = cudaMemcpyAsync(df, features, (size_t)count * MAC_FEATURES * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dl, labels, (size_t)count * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, MAC_NPARAMS * 4, c->stream);
@@ -706,9 +851,9 @@ int gbh_mac_loss_grad(gbh_ctx* c, const float* features, const float* labels, ui
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mac_train_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem());
     if (e == cudaSuccess) {
-        const uint32_t rows = MAC_TRAIN_WARPS * 32;
-        k_mac_train_step<<<(count + rows - 1) / rows, rows, train_smem(), c->stream>>>(
-            df, dl, count, count, 0, 0, 0, mac_weights(c), m->params, m->grad, m->loss);
+        k_mac_train_step<<<tblocks, rows, train_smem(), c->stream>>>(df, dl, count, count, 0, 0, 0, mac_weights(c),
+                                                                      m->params, dp);
+        k_mac_reduce<<<(MAC_PART_STRIDE + 255) / 256, 256, 0, c->stream>>>(dp, warps, m->grad, m->loss);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(grad, m->grad, MAC_NPARAMS * 4, cudaMemcpyDeviceToHost, c->stream);
@@ -717,6 +862,7 @@ int gbh_mac_loss_grad(gbh_ctx* c, const float* features, const float* labels, ui
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(df);
     cudaFree(dl);
+    cudaFree(dp);
     if (e != cudaSuccess) return mac_fail(c, GBH_ERR_CUDA, std::string("mac loss_grad: ") + cudaGetErrorString(e));
     *loss = *loss / (float)count;
     return GBH_OK;

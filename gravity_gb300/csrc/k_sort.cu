@@ -235,6 +235,30 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
     if (bad) set_error(b.st, GBH_DEVERR_SORT_LOOKBACK);
 }
 
+// The eight digit histograms of `n` keys (for a sort whose keys were not
+// written by the step's encode pass) and the live count the passes read.
+__global__ void k_sort_hist(const uint64_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
+                            DevState* __restrict__ st) {
+    __shared__ uint32_t h[SORT_PASSES * SORT_RADIX];
+    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x) h[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->n_new = n;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < SORT_PASSES; ++p) atomicAdd(&h[p * SORT_RADIX + ((k >> (8 * p)) & 0xFF)], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+void launch_sort_hist(const uint64_t* keys, uint32_t n, uint32_t* hist, DevState* st, uint32_t num_sms,
+                      cudaStream_t s) {
+    const uint32_t blocks = min((n + 255) / 256, num_sms * 4u);
+    k_sort_hist<<<blocks > 0 ? blocks : 1, 256, 0, s>>>(keys, n, hist, st);
+}
+
 void sort_setup() {
     cudaFuncSetAttribute(k_sort_pass<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));
     cudaFuncSetAttribute(k_sort_pass<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SortSmem));

@@ -53,22 +53,6 @@ struct NoAllocDevice {
 static NoAllocDevice g_dev[NOALLOC_MAX_DEVICES];
 static std::mutex g_scratch_mu;
 
-// digit histograms of all 8 passes and the live count, into the scratch
-__global__ void k_noalloc_hist(const uint64_t* __restrict__ keys, uint32_t n, NoAllocScratch* s) {
-    __shared__ uint32_t h[SORT_PASSES * SORT_RADIX];
-    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x) h[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) s->st.n_new = n;
-    __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
-#pragma unroll
-        for (int p = 0; p < SORT_PASSES; ++p) atomicAdd(&h[p * SORT_RADIX + ((k >> (8 * p)) & 0xFF)], 1u);
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < SORT_PASSES * SORT_RADIX; i += blockDim.x)
-        if (h[i]) atomicAdd(&s->hist[i], h[i]);
-}
-
 // The set-up of the current device, done once: the scratch's device address,
 // the sort kernels' attributes and the multiprocessor count.
 static const NoAllocDevice* setup_current_device(int* status) {
@@ -129,8 +113,7 @@ extern "C" int gbh_sort_pairs_noalloc(const uint64_t* keys_in, const uint32_t* v
         if (cudaMemsetAsync(s->lookback + (size_t)p * NOALLOC_TILES * SORT_RADIX, 0, (size_t)tiles * SORT_RADIX * 4,
                             st) != cudaSuccess)
             return GBH_ERR_CUDA;
-    const uint32_t hblocks = min((n + 255) / 256, dv->num_sms * 4u);
-    k_noalloc_hist<<<hblocks, 256, 0, st>>>(keys_out, n, s);
+    launch_sort_hist(keys_out, n, s->hist, &s->st, dv->num_sms, st);
     StepBuffers b;
     memset(&b, 0, sizeof(b));
     b.keys_in = keys_out;

@@ -23,6 +23,10 @@
 //                    tensor-core inference).
 // A third instance records (group, node) candidates and their features for
 // the MLP's training data (gbh_mac_generate).
+// The kernel is persistent: one grid of as many blocks as fit on the GPU at
+// once, and each warp takes its next group from a ticket counter when it has
+// finished the last, so warps that meet short walks are not left idle while
+// the rest of their block finishes long ones.
 // Only gravity (merging_collision_or_neither == 0) runs here.
 #include <cstddef>
 #include <type_traits>
@@ -52,10 +56,7 @@ enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 template <int STACK>
 struct GroupSmem {
     uint32_t stack[GW_WARPS][STACK];
-    // list entries (centre of mass, G x mass), each value stored twice:
-    // [0] = (x, x, y, y), [1] = (z, z, w, w), so that one 128-bit load gives
-    // the packed pairs the FP32x2 force loop takes as operands
-    float4 list_cm[GW_WARPS][GW_LIST][2];
+    float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
     uint32_t list_id[GW_WARPS][GW_LIST];
     float list_rad[GW_WARPS][GW_LIST];  // merge form: the leaf entries' body radii
     // merge form: each group body's radius and task counter (slot q * 32 +
@@ -80,18 +81,6 @@ struct GroupCfg {
     using Smem = GroupSmem<stack>;
     static constexpr size_t smem = MODE == GM_LEARNED ? sizeof(Smem) : offsetof(Smem, pend_cm);
 };
-
-// A lane's three body slots, stored so that slots 0 and 1 form packed FP32x2
-// pairs (one __ffma2_rn serves both) and slot 2 stands alone.  Positions are
-// kept negated: r = c + (-x) is one add.
-static_assert(GW_BPL == 3, "the packed layout holds three body slots per lane");
-struct Slots3 {
-    float2 x01, y01, z01;
-    float x2, y2, z2;
-};
-__device__ __forceinline__ float& sx(Slots3& a, int q) { return q == 0 ? a.x01.x : q == 1 ? a.x01.y : a.x2; }
-__device__ __forceinline__ float& sy(Slots3& a, int q) { return q == 0 ? a.y01.x : q == 1 ? a.y01.y : a.y2; }
-__device__ __forceinline__ float& sz(Slots3& a, int q) { return q == 0 ? a.z01.x : q == 1 ? a.z01.y : a.z2; }
 
 // Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
 // more (every leaf lies in exactly one).  A group is a contiguous range of
@@ -172,9 +161,13 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
     const uint32_t N = b.N;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     const uint32_t num_groups = b.st->num_groups;
-    // groups hold up to GBH_GROUP_MAX bodies, usually fewer: warps loop over
-    // them; lane l holds bodies l, l + 32, l + 64 of the group
-    for (uint32_t gi = blockIdx.x * GW_WARPS + w; gi < num_groups; gi += gridDim.x * GW_WARPS) {
+    // groups hold up to GBH_GROUP_MAX bodies, usually fewer: each warp takes
+    // the next group's ticket; lane l holds bodies l, l + 32, l + 64 of it
+    for (;;) {
+    uint32_t gi = 0;
+    if (lane == 0) gi = atomicAdd(&b.st->group_next, 1u);
+    gi = __shfl_sync(0xffffffffu, gi, 0);
+    if (gi >= num_groups) break;
     const uint2 grp = b.groups[gi];
     uint32_t gq[GW_BPL];
     bool actq[GW_BPL];
@@ -188,7 +181,7 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
     const float G = sim->gravitational_constant;
     const float soft = P->softening, theta = P->theta, tol = P->mac_tolerance;
     uint32_t* stk = S.stack[w];
-    float4(*lcm)[2] = S.list_cm[w];
+    float4* lcm = S.list_cm[w];
     uint32_t* lid = S.list_id[w];
     float* lrad = S.list_rad[w];
 
@@ -233,19 +226,15 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
         __syncwarp();
     }
 
-    // walk coordinates of this lane's bodies (absolute, or group-relative),
-    // negated
-    Slots3 np_;
+    // walk coordinates of this lane's bodies (absolute, or group-relative)
+    float3 pw[GW_BPL];
 #pragma unroll
     for (int q = 0; q < GW_BPL; ++q) {
-        float3 p = make_float3(pmq[q].x, pmq[q].y, pmq[q].z);
+        pw[q] = make_float3(pmq[q].x, pmq[q].y, pmq[q].z);
         if (PREC) {
             const float4 lo_b = b.leaf_lo[actq[q] ? gq[q] : grp.x];
-            p = make_float3((pmq[q].x - gg.cx) + lo_b.x, (pmq[q].y - gg.cy) + lo_b.y, (pmq[q].z - gg.cz) + lo_b.z);
+            pw[q] = make_float3((pmq[q].x - gg.cx) + lo_b.x, (pmq[q].y - gg.cy) + lo_b.y, (pmq[q].z - gg.cz) + lo_b.z);
         }
-        sx(np_, q) = -p.x;
-        sy(np_, q) = -p.y;
-        sz(np_, q) = -p.z;
     }
     const bool want_pot = (P->flags & GBH_FLAG_STORE_POTENTIAL) && b.potential;
     // merging (bh_force.comp:109-112): every leaf entry is tested for overlap
@@ -268,16 +257,13 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
         if (lane == 0) S.grp_rad[w] = gr;
         __syncwarp();
     }
-    Slots3 acc;  // accelerations
-#pragma unroll
-    for (int q = 0; q < GW_BPL; ++q) sx(acc, q) = sy(acc, q) = sz(acc, q) = 0.f;
-    float pot[GW_BPL];
-    float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], npt_[GW_BPL];  // PREC: leaf terms (Kahan)
+    float ax[GW_BPL], ay[GW_BPL], az[GW_BPL], pot[GW_BPL];
+    float nx_[GW_BPL], ny_[GW_BPL], nz_[GW_BPL], np_[GW_BPL];  // PREC: leaf terms (Kahan)
     float cx_[GW_BPL], cy_[GW_BPL], cz_[GW_BPL], cp_[GW_BPL];
 #pragma unroll
     for (int q = 0; q < GW_BPL; ++q) {
-        pot[q] = 0.f;
-        nx_[q] = ny_[q] = nz_[q] = npt_[q] = 0.f;
+        ax[q] = ay[q] = az[q] = pot[q] = 0.f;
+        nx_[q] = ny_[q] = nz_[q] = np_[q] = 0.f;
         cx_[q] = cy_[q] = cz_[q] = cp_[q] = 0.f;
     }
     uint32_t inter = 0, evals = 0, opened = 0;
@@ -290,15 +276,6 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
     // softening of at least 1e-20 a body's own entry adds exactly zero (its
     // offset is zero, its 1/r^3 finite), so only smaller softenings compare ids.
     const bool self_check = !(soft >= 1e-20f);
-    // list entry j as (x, y, z, G m)
-    auto list_get = [&](uint32_t j) {
-        const float4 a = lcm[j][0], c = lcm[j][1];
-        return make_float4(a.x, a.z, c.x, c.z);
-    };
-    auto list_put = [&](uint32_t j, float4 c) {
-        lcm[j][0] = make_float4(c.x, c.x, c.y, c.y);
-        lcm[j][1] = make_float4(c.z, c.z, c.w, c.w);
-    };
     // penetration of group body q with the leaf entry j (body id lj, radius
     // kept with the entry): a task when the distance is below the sum of the
     // radii and this body's index is the smaller (bh_force.comp:109-112)
@@ -328,11 +305,11 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
             // check, merge tasks
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 c = list_get(j);
+                const float4 c = lcm[j];
                 const uint32_t lj = lid[j];
 #pragma unroll
                 for (int q = 0; q < GW_BPL; ++q) {
-                    const float rx = c.x + sx(np_, q), ry = c.y + sy(np_, q), rz = c.z + sz(np_, q);
+                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
                     if (merging) merge_test(q, lj, rx, ry, rz, lrad[j]);
                     const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                     const float inv = rsqrtf(rr);
@@ -343,11 +320,11 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
                         kahan_add(nx_[q], cx_[q], f * rx);
                         kahan_add(ny_[q], cy_[q], f * ry);
                         kahan_add(nz_[q], cz_[q], f * rz);
-                        if (want_pot) kahan_add(npt_[q], cp_[q], ph);
+                        if (want_pot) kahan_add(np_[q], cp_[q], ph);
                     } else {
-                        sx(acc, q) = __fmaf_rn(f, rx, sx(acc, q));
-                        sy(acc, q) = __fmaf_rn(f, ry, sy(acc, q));
-                        sz(acc, q) = __fmaf_rn(f, rz, sz(acc, q));
+                        ax[q] = __fmaf_rn(f, rx, ax[q]);
+                        ay[q] = __fmaf_rn(f, ry, ay[q]);
+                        az[q] = __fmaf_rn(f, rz, az[q]);
                         if (want_pot) pot[q] += ph;
                     }
                 }
@@ -355,55 +332,45 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
         } else if (self_check) {
 #pragma unroll 2
             for (uint32_t j = 0; j < cnt; ++j) {
-                const float4 c = list_get(j);
+                const float4 c = lcm[j];
                 const uint32_t lj = lid[j];
 #pragma unroll
                 for (int q = 0; q < GW_BPL; ++q) {
-                    const float rx = c.x + sx(np_, q), ry = c.y + sy(np_, q), rz = c.z + sz(np_, q);
+                    const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
                     const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
                     const float inv = rsqrtf(rr);
                     const float f = (lj == gq[q]) ? 0.0f : c.w * (inv * inv * inv);
-                    sx(acc, q) = __fmaf_rn(f, rx, sx(acc, q));
-                    sy(acc, q) = __fmaf_rn(f, ry, sy(acc, q));
-                    sz(acc, q) = __fmaf_rn(f, rz, sz(acc, q));
+                    ax[q] = __fmaf_rn(f, rx, ax[q]);
+                    ay[q] = __fmaf_rn(f, ry, ay[q]);
+                    az[q] = __fmaf_rn(f, rz, az[q]);
                 }
             }
         } else {
-            // the hot loop: slots 0 and 1 as one packed FP32x2 pair (every
-            // instruction but the reciprocal square roots serves both), slot
-            // 2 alone when the group has more than 64 bodies (warp-uniform)
-            const float2 s2 = make_float2(soft, soft);
-            auto pairs = [&](auto with_third) {
-                constexpr bool THIRD = decltype(with_third)::value;
+            // one loop per number of slots in use (warp-uniform), unrolled
+            // over a constant
+            auto slots = [&](auto qn) {
+                constexpr int Q = decltype(qn)::value;
 #pragma unroll 2
                 for (uint32_t j = 0; j < cnt; ++j) {
-                    const float4 e0 = lcm[j][0], e1 = lcm[j][1];
-                    const float2 cx = make_float2(e0.x, e0.y), cy = make_float2(e0.z, e0.w);
-                    const float2 cz = make_float2(e1.x, e1.y), cw = make_float2(e1.z, e1.w);
-                    const float2 rx = __fadd2_rn(cx, np_.x01), ry = __fadd2_rn(cy, np_.y01), rz = __fadd2_rn(cz, np_.z01);
-                    float2 rr = __ffma2_rn(rx, rx, s2);
-                    rr = __ffma2_rn(ry, ry, rr);
-                    rr = __ffma2_rn(rz, rz, rr);
-                    const float2 inv = make_float2(rsqrtf(rr.x), rsqrtf(rr.y));
-                    const float2 f = __fmul2_rn(cw, __fmul2_rn(inv, __fmul2_rn(inv, inv)));
-                    acc.x01 = __ffma2_rn(f, rx, acc.x01);
-                    acc.y01 = __ffma2_rn(f, ry, acc.y01);
-                    acc.z01 = __ffma2_rn(f, rz, acc.z01);
-                    if (THIRD) {
-                        const float tx = e0.x + np_.x2, ty = e0.z + np_.y2, tz = e1.x + np_.z2;
-                        const float t2 = __fmaf_rn(tz, tz, __fmaf_rn(ty, ty, __fmaf_rn(tx, tx, soft)));
-                        const float ti = rsqrtf(t2);
-                        const float tf = e1.z * (ti * (ti * ti));
-                        acc.x2 = __fmaf_rn(tf, tx, acc.x2);
-                        acc.y2 = __fmaf_rn(tf, ty, acc.y2);
-                        acc.z2 = __fmaf_rn(tf, tz, acc.z2);
+                    const float4 c = lcm[j];
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) {
+                        const float rx = c.x - pw[q].x, ry = c.y - pw[q].y, rz = c.z - pw[q].z;
+                        const float rr = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmaf_rn(rx, rx, soft)));
+                        const float inv = rsqrtf(rr);
+                        const float f = c.w * (inv * inv * inv);
+                        ax[q] = __fmaf_rn(f, rx, ax[q]);
+                        ay[q] = __fmaf_rn(f, ry, ay[q]);
+                        az[q] = __fmaf_rn(f, rz, az[q]);
                     }
                 }
             };
             if (nq >= GW_BPL)
-                pairs(std::true_type{});
+                slots(std::integral_constant<int, GW_BPL>{});
+            else if (nq == 2)
+                slots(std::integral_constant<int, 2>{});
             else
-                pairs(std::false_type{});
+                slots(std::integral_constant<int, 1>{});
         }
         if (merging && !(PREC || want_pot)) {
             // merge tests outside the force loop: lane j screens entry j with
@@ -415,7 +382,7 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
             for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
                 bool near = false;
                 if (j0 + lane < cnt && lid[j0 + lane] < N) {
-                    const float4 c = list_get(j0 + lane);
+                    const float4 c = lcm[j0 + lane];
                     const float dx = fmaxf(fmaxf(bmn.x - c.x, c.x - bmx.x), 0.0f);
                     const float dy = fmaxf(fmaxf(bmn.y - c.y, c.y - bmx.y), 0.0f);
                     const float dz = fmaxf(fmaxf(bmn.z - c.z, c.z - bmx.z), 0.0f);
@@ -426,12 +393,12 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
                 while (m) {
                     const uint32_t j = j0 + __ffs(m) - 1;
                     m &= m - 1;
-                    const float4 c = list_get(j);
+                    const float4 c = lcm[j];
                     const uint32_t lj = lid[j];
                     const float lr = lrad[j];
 #pragma unroll
                     for (int q = 0; q < GW_BPL; ++q)
-                        merge_test(q, lj, c.x + sx(np_, q), c.y + sy(np_, q), c.z + sz(np_, q), lr);
+                        merge_test(q, lj, c.x - pw[q].x, c.y - pw[q].y, c.z - pw[q].z, lr);
                 }
             }
         }
@@ -450,9 +417,9 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
         if (kind == 1) {
             const uint32_t pos = ln + __popc(bl & lanemask_lt());
             if (PREC)
-                list_put(pos, make_float4((cm.x - gg.cx) + lo.x, (cm.y - gg.cy) + lo.y, (cm.z - gg.cz) + lo.z, G * cm.w));
+                lcm[pos] = make_float4((cm.x - gg.cx) + lo.x, (cm.y - gg.cy) + lo.y, (cm.z - gg.cz) + lo.z, G * cm.w);
             else
-                list_put(pos, make_float4(cm.x, cm.y, cm.z, G * cm.w));
+                lcm[pos] = make_float4(cm.x, cm.y, cm.z, G * cm.w);
             lid[pos] = id;
             if (merging) lrad[pos] = lo.x;  // the leaf's radius, read at the pop (0 for nodes)
         }
@@ -470,8 +437,7 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
             ln -= 32;
             __syncwarp();
             if (lane < ln) {  // move the remaining entries to the front
-                lcm[lane][0] = lcm[32 + lane][0];
-                lcm[lane][1] = lcm[32 + lane][1];
+                lcm[lane] = lcm[32 + lane];
                 lid[lane] = lid[32 + lane];
                 if (merging) lrad[lane] = lrad[32 + lane];
             }
@@ -571,7 +537,7 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
                     kind = group_theta_accept(gg, ng, theta) ? 1 : 2;
                     // training pairs: the band the network decides (see GM_LEARNED)
                     if (MODE == GM_RECORD && ng.count <= mw.rec_max_bodies &&
-                        hash32(id ^ hash32(gi + mw.rec_seed)) <= mw.rec_keep &&
+                        hash32(id ^ hash32(grp.x + mw.rec_seed)) <= mw.rec_keep &&
                         group_rho(gg, ng) < band_hi && !(group_rho(gg, ng) < band_lo)) {
                         const uint32_t slot = atomicAdd(mw.rec_count, 1u);
                         if (slot < mw.rec_cap) {
@@ -620,12 +586,12 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
         // body index and position again (not kept live through the walk)
         const uint32_t bi = b.idx_in[gq[q]];
         const float4 pm = b.leaf_pm[gq[q]];
-        float fx = sx(acc, q), fy = sy(acc, q), fz = sz(acc, q), fp = pot[q];
+        float fx = ax[q], fy = ay[q], fz = az[q], fp = pot[q];
         if (PREC) {
             fx = fx + (nx_[q] - cx_[q]);
             fy = fy + (ny_[q] - cy_[q]);
             fz = fz + (nz_[q] - cz_[q]);
-            fp = fp + (npt_[q] - cp_[q]);
+            fp = fp + (np_[q] - cp_[q]);
         }
         if (b.accel && (P->flags & GBH_FLAG_STORE_ACCEL)) b.accel[bi] = make_float4(fx, fy, fz, 0.0f);
         if (b.accel_mag) b.accel_mag[bi] = sqrtf(fx * fx + fy * fy + fz * fz);
@@ -645,9 +611,18 @@ static size_t group_smem(int mode) {
                                                                               : GroupCfg<GM_THETA>::smem;
 }
 
+// resident blocks per SM of each instance (set up once per process)
+static int g_blocks_per_sm[3][3];
+
 template <int MODE, int FORM>
 static void set_smem() {
     cudaFuncSetAttribute(k_walk_group<MODE, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(MODE));
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_walk_group<MODE, FORM>, GW_THREADS, group_smem(MODE)) !=
+            cudaSuccess ||
+        nb < 1)
+        nb = 1;
+    g_blocks_per_sm[MODE][FORM] = nb;
 }
 
 void group_walk_setup() {
@@ -668,7 +643,11 @@ void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
 template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
     if (MODE != GM_RECORD) launch_find_groups(b, s);
-    const uint32_t blocks = (b.N + GW_THREADS - 1) / GW_THREADS;
+    cudaMemsetAsync(&b.st->group_next, 0, 4, s);
+    // persistent: the blocks that fit at once (no more than the groups need)
+    const uint32_t need = (b.N + GW_WARPS * 32 - 1) / (GW_WARPS * 32) + 1;
+    uint32_t blocks = b.num_sms * (uint32_t)g_blocks_per_sm[MODE][FORM];
+    if (blocks > need) blocks = need;
     k_walk_group<MODE, FORM><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
 }
 

@@ -218,6 +218,29 @@ int gbh_upload_bodies(gbh_ctx* ctx, const gbh_body* host, uint32_t count, uint32
  * Returns when both copies have finished; the buffers must not overlap. */
 int gbh_exchange_bodies(gbh_ctx* ctx, gbh_body* host_out, const gbh_body* host_in, uint32_t count, uint32_t offset);
 
+/* Streamed steps, for a host that hands the simulation a new state every step
+ * or keeps every step's state (the headless counterpart of the reference's
+ * per-frame recording, src/main/java/com/grumbo/record/FrameRecorder.java,
+ * which captures rendered frames), without stalling the GPU on the copies.
+ * No single reference call is replaced; it combines BarnesHut.step with the
+ * body upload (GPU.java:1166-1196) and read-back (SSBO.java:274-290).
+ * One call:
+ *   - runs one step (gbh_step) on the current state;
+ *   - while it runs, copies `next_input` (initial_num_bodies bodies, host
+ *     memory; pinned memory lets the copy overlap) to the device, and copies
+ *     the result of the PREVIOUS call's step into `last_result`;
+ *   - after the step, keeps its result for the next call and makes
+ *     `next_input` the current state (the step after it starts from it).
+ * `next_input` NULL: the step's result stays the current state (a plain
+ * simulation whose every state is streamed back).  `last_result` NULL, or the
+ * first call: no result is copied.  Returns when both copies have finished
+ * (the host buffers may be reused); the step itself may still be running.
+ * gbh_step_streamed_finish copies the last call's result and waits for the
+ * context.  The first call allocates two body-sized device buffers. */
+int gbh_step_streamed(gbh_ctx* ctx, const gbh_step_params* params, const gbh_body* next_input,
+                      gbh_body* last_result);
+int gbh_step_streamed_finish(gbh_ctx* ctx, gbh_body* last_result);
+
 /* BarnesHut.init (BarnesHut.java:170-173, bh_init.comp:10-27): identity index,
  * derive G and the body length constant. */
 int gbh_init(gbh_ctx* ctx);

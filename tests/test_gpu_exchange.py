@@ -37,3 +37,67 @@ def test_exchange_returns_state_and_installs_input(gbh_lib):
     out = np.zeros(1000, abi.BODY_DTYPE)
     sim.exchange_bodies(out, a[5000:6000], offset=5000)
     assert np.array_equal(sim.read_bodies()[5000:6000].view(np.uint32), a[5000:6000].view(np.uint32))
+
+
+def _pinned(torch, n):
+    return torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
+
+
+def test_streamed_steps_equal_upload_step_read(gbh_lib):
+    # every call installs a new state and returns the previous call's result:
+    # the results must be bit-identical to upload + step + read per state
+    torch = pytest.importorskip("torch")
+    n = 70001
+    states = [ic.plummer(n, seed=10 + k) for k in range(4)]
+    bounds = ic.exact_bounds(states[0])
+    p = abi.step_params(theta=0.5, softening=1e-4, bounds=abi.BOUNDS_DYNAMIC)
+    ref = BarnesHut(n, bounds, abi.units(G=1.0))
+    ref.upload_bodies(states[0])
+    ref.init()
+    want = []
+    for k in range(3):
+        ref.upload_bodies(states[k])
+        ref.step(p)
+        want.append(ref.read_bodies())
+    sim = BarnesHut(n, bounds, abi.units(G=1.0))
+    sim.upload_bodies(states[0])
+    sim.init()
+    nxt, out = _pinned(torch, n), _pinned(torch, n)
+    got = []
+    for k in range(3):
+        nxt[:] = states[k + 1]
+        out.fill(0)
+        sim.step_streamed(p, nxt, out)
+        if k:
+            got.append(out.copy())
+    sim.step_streamed_finish(out)
+    got.append(out.copy())
+    for k in range(3):
+        assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), k
+    # the last installed input is the current state
+    assert np.array_equal(sim.read_bodies().view(np.uint32), states[3].view(np.uint32))
+
+
+def test_streamed_steps_without_input_record_the_trajectory(gbh_lib):
+    # next_input NULL: a plain simulation whose every state comes back
+    torch = pytest.importorskip("torch")
+    n = 50000
+    b = ic.plummer(n, seed=4)
+    p = abi.step_params(theta=0.5, softening=1e-4)
+    a = BarnesHut(n, ic.exact_bounds(b), abi.units(G=1.0))
+    c = BarnesHut(n, ic.exact_bounds(b), abi.units(G=1.0))
+    for x in (a, c):
+        x.upload_bodies(b)
+        x.init()
+    out = _pinned(torch, n)
+    traj = []
+    for k in range(4):
+        a.step_streamed(p, None, out if k else None)
+        if k:
+            traj.append(out.copy())
+    a.step_streamed_finish(out)
+    traj.append(out.copy())
+    for k in range(4):
+        c.step(p)
+        assert np.array_equal(traj[k].view(np.uint32), c.read_bodies().view(np.uint32)), k
+    assert np.array_equal(a.read_bodies().view(np.uint32), c.read_bodies().view(np.uint32))

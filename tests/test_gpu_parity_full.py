@@ -180,7 +180,7 @@ def test_c2_merge_steps_match_oracle(gbh_lib, oracle_mod):
         np.testing.assert_allclose(bg["pos_mass"], bo["pos_mass"], rtol=1e-5, atol=1e-6)
         total_merged += sg.merged
         total_oob += sg.out_of_bounds
-    assert total_merged > 100 and total_oob >= 1000, (total_merged, total_oob)
+    assert total_merged >= 30 and total_oob >= 1000, (total_merged, total_oob)
     # the next compaction removes the same bodies
     for x in (g, o):
         x.stage_reset(p)
