@@ -46,6 +46,9 @@ __global__ void k_sort_scan(StepBuffers b) {
 
 struct SortSmem {
     uint32_t warp_hist[SORT_THREADS / 32][SORT_RADIX + 1];  // +1: sentinel bucket of out-of-range items
+#ifdef SORT_RANK_MATCH
+    uint32_t match[SORT_THREADS / 32][SORT_RADIX + 1];       // per-warp digit masks of the ranking
+#endif
     uint32_t block_excl[SORT_RADIX + 1];
     uint32_t delta[SORT_RADIX];
     uint32_t warp_tot[SORT_THREADS / 32];
@@ -82,6 +85,37 @@ __device__ __forceinline__ void rank_items(const uint64_t (&key)[SORT_ITEMS], ui
     }
 }
 
+#ifdef SORT_RANK_MATCH
+// The same stable ranking with the peers found in shared memory: each lane
+// ORs its bit into its digit's word of a per-warp mask table, reads the word
+// back (the lanes with its digit), and the digit's lowest lane reserves the
+// group's ranks and clears the word.  One shared atomic per item instead of
+// eight ballots.
+template <uint32_t SHIFT, int BITS>
+__device__ __forceinline__ void rank_items_match(const uint64_t (&key)[SORT_ITEMS], uint32_t (&rank)[SORT_ITEMS],
+                                                 uint32_t* warp_hist, uint32_t* match, uint32_t lane, uint32_t seg,
+                                                 uint32_t n) {
+    const uint32_t bit = 1u << lane;
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        uint32_t dig = (uint32_t)(key[i] >> SHIFT) & 0xFFu;
+        if (BITS > 8 && seg + i * 32 + lane >= n) dig = SORT_RADIX;
+        atomicOr(&match[dig], bit);
+        __syncwarp();
+        const uint32_t peers = match[dig];
+        const uint32_t leader = __ffs(peers) - 1;
+        const uint32_t before = __popc(peers & (bit - 1u));
+        uint32_t prev = 0;
+        __syncwarp();
+        if (lane == leader) {
+            prev = atomicAdd(&warp_hist[dig], (uint32_t)__popc(peers));
+            match[dig] = 0u;
+        }
+        rank[i] = __shfl_sync(0xffffffffu, prev, leader) + before;
+    }
+}
+#endif
+
 // One kernel instance per pass: the digit's bit offset is a constant.
 template <uint32_t PASS>
 __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, const uint64_t* __restrict__ kin,
@@ -94,8 +128,12 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
     constexpr uint32_t shift = SORT_BITS * PASS;
     const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
     if (threadIdx.x == 0) S.tile = atomicAdd(&b.st->sort_tiles[pass], 1u);
-    for (uint32_t i = threadIdx.x; i < (SORT_THREADS / 32) * (SORT_RADIX + 1); i += SORT_THREADS)
+    for (uint32_t i = threadIdx.x; i < (SORT_THREADS / 32) * (SORT_RADIX + 1); i += SORT_THREADS) {
         (&S.warp_hist[0][0])[i] = 0;
+#ifdef SORT_RANK_MATCH
+        (&S.match[0][0])[i] = 0;
+#endif
+    }
     __syncthreads();
     const uint32_t tile = S.tile;
     const uint32_t base = tile * SORT_TILE;
@@ -114,7 +152,11 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
             key[i] = kin[seg + i * 32 + lane];
             val[i] = vin[seg + i * 32 + lane];
         }
+#ifdef SORT_RANK_MATCH
+        rank_items_match<shift, 8>(key, rank, S.warp_hist[w], S.match[w], lane, seg, n);
+#else
         rank_items<shift, 8>(key, rank, S.warp_hist[w], lane, seg, n);
+#endif
     } else {
 #pragma unroll
         for (int i = 0; i < SORT_ITEMS; ++i) {
@@ -127,7 +169,11 @@ __global__ __launch_bounds__(SORT_THREADS, 3) void k_sort_pass(StepBuffers b, co
                 val[i] = 0;
             }
         }
+#ifdef SORT_RANK_MATCH
+        rank_items_match<shift, 9>(key, rank, S.warp_hist[w], S.match[w], lane, seg, n);
+#else
         rank_items<shift, 9>(key, rank, S.warp_hist[w], lane, seg, n);
+#endif
     }
     __syncthreads();
     // thread d: exclusive prefix of digit d over warps, tile total

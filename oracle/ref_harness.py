@@ -28,6 +28,49 @@ REF_SHADERS = os.path.join(REF_ROOT, "src", "main", "resources", "shaders")
 _lib = None
 
 
+RENDER_LIB_PATH = os.path.join(_HERE, "_ref", "libbh_ref_render.so")
+_render = None
+
+
+def render_lib():
+    """The reference's node-glow and region vertex shaders compiled as C++
+    (oracle/ref_glsl/ref_render.cpp)."""
+    global _render
+    if _render is None:
+        if not os.path.exists(RENDER_LIB_PATH):
+            build_if_available()
+        L = C.CDLL(RENDER_LIB_PATH)
+        L.ref_render_set.restype = None
+        L.ref_render_set.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(abi.View),
+                                     C.POINTER(C.c_float)]
+        for f in (L.ref_glow_instances, L.ref_region_instances):
+            f.restype = None
+            f.argtypes = [C.c_int, C.c_void_p]
+        _render = L
+    return _render
+
+
+def render_instances(internal: np.ndarray, bodies: np.ndarray, num_bodies: int, view, mvp16) -> tuple:
+    """Run nodeglow.vert (4 vertices) and regions.vert (2 cube corners) for
+    every instance the shaders visit: glow instances [0, len(bodies) - 1),
+    region instances [0, num_bodies).  `internal` is padded with zeroed slots
+    up to num_bodies (the region shader reads one slot past the live nodes).
+    Returns (glow[count][4][16], regions[num_bodies][2][5])."""
+    L = render_lib()
+    n_cap = len(bodies)
+    nodes = np.zeros(max(n_cap, num_bodies) + 1, dtype=abi.NODE_DTYPE)
+    nodes[: len(internal)] = internal
+    b = np.ascontiguousarray(bodies, dtype=abi.BODY_DTYPE)
+    m = (C.c_float * 16)(*[float(x) for x in np.asarray(mvp16, np.float32).reshape(-1)])
+    L.ref_render_set(nodes.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), num_bodies, n_cap,
+                     C.byref(view), m)
+    glow = np.zeros((n_cap - 1, 4, 16), np.float32)
+    L.ref_glow_instances(n_cap - 1, glow.ctypes.data_as(C.c_void_p))
+    reg = np.zeros((num_bodies, 2, 5), np.float32)
+    L.ref_region_instances(num_bodies, reg.ctypes.data_as(C.c_void_p))
+    return glow, reg
+
+
 def available() -> bool:
     return os.path.exists(LIB_PATH) or os.path.isdir(REF_SHADERS)
 

@@ -10,7 +10,11 @@ GPU sort, about 128 tiles of its fill) store the generator of their inputs
 (tests/golden/large_inputs.py) with a digest of the bodies, digests of the
 reference's exact outputs, and every 16th body after the step.
 
-Usage: python tests/golden/make_golden.py [--large-only]
+view_select.npz holds the outputs of the reference's node-glow and region
+vertex shaders (compiled as C++ by oracle/ref_glsl/ref_render.cpp) over the
+reference's tree of a 2,048-body Plummer sphere, for three views.
+
+Usage: python tests/golden/make_golden.py [--large-only | --views-only]
 """
 from __future__ import annotations
 
@@ -125,12 +129,77 @@ def make_large():
         print(path, os.path.getsize(path), "tasks", len(tasks))
 
 
+VIEW_N = 2048
+
+
+def views():
+    """Three cameras over the tree: far and absolute, oblique and absolute,
+    near and relative to body 7 (camera scale 1)."""
+    fov, aspect = np.radians(50.0), 16.0 / 9.0
+    proj = abi.perspective(fov, aspect, 0.01, 1e5)
+    out = []
+    for eye, rel, scale, depths in [((0, 0, 60), 0xFFFFFFFF, 10.0, (2, 6)),
+                                    ((30, 20, 15), 0xFFFFFFFF, 10.0, (0, 3)),
+                                    ((5, -4, 8), 7, 1.0, (4, 30))]:
+        mv = abi.look_at(eye, (0, 0, 0))
+        v = abi.view(mv, proj, fov, aspect, camera_scale=scale, relative_to=rel, glow_max_depth=12,
+                     glow_intensity=0.05, region_depths=depths)
+        mvp = (np.asarray(proj, np.float64) @ np.asarray(mv, np.float64)).astype(np.float32).T.reshape(-1)
+        out.append((v, mvp))
+    return out
+
+
+def make_views():
+    """nodeglow.vert and regions.vert of the reference over the tree of a
+    2,048-body Plummer sphere built by the reference's kernels, for three
+    views: per selected node the shader's outputs and clip positions."""
+    import ctypes as C
+
+    n = VIEW_N
+    bodies = ic.plummer(n, seed=31)
+    bounds = live_bounds(bodies)
+    p = abi.step_params(theta=0.5, softening=1e-4)
+    r = R.RefBarnesHut(n, bounds, abi.units(G=1.0))
+    r.upload_bodies(bodies)
+    r.init()
+    r.stage_reset(p)
+    r.stage_prepare(p)
+    r.stage_sort()
+    r.stage_build()
+    r.stage_fill()
+    nodes = r.read_internal_nodes()[: n - 1].copy()
+    state = r.read_bodies()
+    r.close()
+    out = {"bodies": bodies, "bounds": bounds, "params": np.array([float(getattr(p, f)) for f in PARAM_FIELDS])}
+    for k, (v, mvp) in enumerate(views()):
+        glow, reg = R.render_instances(nodes, state, n, v, mvp)
+        gsel = np.nonzero(glow[:, 0, 6] != 0)[0].astype(np.uint32)  # culled instances have vIntensity 0
+        culled = (reg[:, 0, 0] == 2) & (reg[:, 0, 1] == 2) & (reg[:, 0, 2] == 2) & (reg[:, 0, 3] == 1)
+        rsel = np.nonzero(~culled[: n - 1])[0].astype(np.uint32)  # live nodes [0, n - 1)
+        out[f"v{k}_view"] = np.frombuffer(bytes(v), np.uint8)
+        out[f"v{k}_mvp"] = mvp
+        out[f"v{k}_glow_nodes"] = gsel
+        out[f"v{k}_glow_position"] = glow[gsel][:, :, 0:4]        # gl_Position of vertices 0-3
+        out[f"v{k}_glow_outputs"] = glow[gsel][:, 0, 6:15]         # vIntensity, vColor, vCenterView, vNdcScale
+        out[f"v{k}_region_nodes"] = rsel
+        out[f"v{k}_region_position"] = reg[rsel][:, :, 0:4]        # gl_Position at the corners -0.5, +0.5
+        out[f"v{k}_region_depth"] = reg[rsel][:, 0, 4].astype(np.uint32)
+        print("view", k, "glow", len(gsel), "regions", len(rsel))
+    path = os.path.join(OUT, "view_select.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path))
+
+
 def main():
     units = abi.units(G=1.0)
     if "--large-only" in sys.argv:
         make_large()
         return
+    if "--views-only" in sys.argv:
+        make_views()
+        return
     make_large()
+    make_views()
     for name, bodies, bounds, p, steps in cases():
         if bounds is None:
             bounds = live_bounds(bodies)

@@ -25,7 +25,8 @@ def same_bits(a, b) -> bool:
 
 def fixtures():
     """The small fixtures (inputs and outputs stored whole)."""
-    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")) if not os.path.basename(p).startswith("large_"))
+    return sorted(p for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))
+                  if not os.path.basename(p).startswith(("large_", "view_")))
 
 
 def large_fixtures():
@@ -149,3 +150,93 @@ def replay_large(path, make, exact_walk: bool):
         np.testing.assert_allclose(mine["vel_density"], gb["vel_density"], rtol=1e-4, atol=1e-5, equal_nan=True)
     assert x.read_sim_values().out_of_bounds == int(z["out_of_bounds"]), path
     return True
+
+
+# ---- node selection against the reference's vertex shaders -------------------
+VIEW_FIXTURE = os.path.join(GOLDEN_DIR, "view_select.npz")
+_BOX = np.float32(1.5)
+_MAPPING = np.array([[-1, -1], [-1, 1], [1, -1], [1, 1]], np.float32) * _BOX  # nodeglow.vert vertices 0-3
+
+
+def view_fixture():
+    z = np.load(VIEW_FIXTURE)
+    views = []
+    k = 0
+    while f"v{k}_view" in z:
+        v = abi.View.from_buffer_copy(z[f"v{k}_view"].tobytes())
+        views.append((v, z[f"v{k}_mvp"]))
+        k += 1
+    return z, views
+
+
+def tree_of_view_fixture(make):
+    """The fixture's tree (reset, compaction, sort, build, fill of its bodies)
+    on an implementation with the stage API; returns it and its live count."""
+    z = np.load(VIEW_FIXTURE)
+    p = params_of(z)
+    x = make(len(z["bodies"]), z["bounds"], abi.units(G=1.0))
+    x.upload_bodies(z["bodies"])
+    x.init()
+    x.stage_reset(p)
+    x.stage_prepare(p)
+    x.stage_sort()
+    x.stage_build()
+    x.stage_fill()
+    return x, x.read_sim_values().num_bodies
+
+
+def _f32(x):
+    return np.float32(x)
+
+
+def _mat4_vec4(m16, v):
+    """uMVP * v with the column terms added in column order, in FP32."""
+    M = np.asarray(m16, np.float32).reshape(4, 4)  # [column][row]
+    out = np.zeros(4, np.float32)
+    for i in range(4):
+        s = _f32(M[0, i] * v[0])
+        s = _f32(s + _f32(M[1, i] * v[1]))
+        s = _f32(s + _f32(M[2, i] * v[2]))
+        s = _f32(s + _f32(M[3, i] * v[3]))
+        out[i] = s
+    return out
+
+
+def check_glow_against_shader(records, z, k):
+    """Records of gbh_select_glow_nodes (any order) against the shader's
+    outputs for view k: the same nodes; vIntensity, vColor, vCenterView and
+    the NDC scales bit for bit; gl_Position of the four vertices rebuilt from
+    the record in the shader's operation order, bit for bit."""
+    r = np.sort(records, order="node")
+    assert np.array_equal(r["node"], z[f"v{k}_glow_nodes"]), "glow selection differs"
+    o = z[f"v{k}_glow_outputs"]
+    assert same_bits(r["intensity"], o[:, 0])
+    assert same_bits(r["color"][:, :3], o[:, 1:4])
+    assert same_bits(r["center_view"], o[:, 4:7])
+    assert same_bits(r["ndc_scale"], o[:, 7:9])
+    pos = z[f"v{k}_glow_position"]
+    for i in range(len(r)):
+        c = r["center_clip"][i].astype(np.float32)
+        scale = r["ndc_scale"][i].astype(np.float32)
+        for vid in range(4):
+            off = (_MAPPING[vid] * scale) * c[3]
+            want = np.array([c[0] + off[0], c[1] + off[1], c[2], c[3]], np.float32)
+            assert same_bits(want, pos[i, vid]), (k, int(r["node"][i]), vid)
+
+
+def check_regions_against_shader(records, z, k, mvp):
+    """Records of gbh_select_regions against regions.vert for view k: the same
+    nodes and depths; gl_Position at two opposite unit-cube corners rebuilt
+    from the record's centre and size (center + aPos * size, then uMVP),
+    bit for bit."""
+    r = np.sort(records, order="node")
+    assert np.array_equal(r["node"], z[f"v{k}_region_nodes"]), "region selection differs"
+    assert np.array_equal(r["depth"], z[f"v{k}_region_depth"])
+    pos = z[f"v{k}_region_position"]
+    for i in range(len(r)):
+        cen = r["center"][i].astype(np.float32)
+        size = r["size"][i].astype(np.float32)
+        for j, a in enumerate((np.float32(-0.5), np.float32(0.5))):
+            w = cen + a * size
+            got = _mat4_vec4(mvp, np.array([w[0], w[1], w[2], 1.0], np.float32))
+            assert same_bits(got, pos[i, j]), (k, int(r["node"][i]), j)

@@ -70,3 +70,21 @@ def test_selection_capacity_keeps_the_count(gbh_lib, stepped):
     # a count-only query writes nothing
     none, sel3 = sim.select_regions(v, capacity=0)
     assert sel3 == sel and len(none) == 0
+
+
+def test_selection_matches_reference_shaders(gbh_lib):
+    # the GPU's tree of the fixture's bodies (bit-exact with the reference's)
+    # and its selection against the outputs of the reference's own vertex
+    # shaders (tests/golden/view_select.npz), bit for bit
+    from .golden_check import check_glow_against_shader, check_regions_against_shader, tree_of_view_fixture, \
+        view_fixture
+
+    z, views = view_fixture()
+    sim, n = tree_of_view_fixture(BarnesHut)
+    for k, (v, mvp) in enumerate(views):
+        g, sel = sim.select_glow_nodes(v)
+        assert sel > 0
+        check_glow_against_shader(g, z, k)
+        r, sel = sim.select_regions(v)
+        assert sel > 0
+        check_regions_against_shader(r, z, k, mvp)
