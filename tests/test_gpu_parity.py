@@ -305,3 +305,62 @@ def test_direct_sum_matches_fp64(gbh_lib, oracle_mod):
     ref = oracle_mod.direct_sum_fp64(b, sample, 1.0, float(p.softening))
     # both FP64 throughout: only the summation order differs
     assert rel_err(got, ref).max() < 1e-11
+
+
+def test_derived_units_and_mid_run_update(gbh_lib, oracle_mod):
+    # G and the body-length constant derived on the device from the unit set
+    # (no override, bh_update.comp:22-25, common.glsl:346-360), then a unit
+    # change in the middle of the run through the step parameters.  Units:
+    # solar mass, astronomical unit, year, stellar density, so G comes out
+    # near 4 pi^2.  CUDA's powf and the oracle's may differ in the last ulp,
+    # so the constants agree to 3e-7; the merge tasks, which depend on the
+    # body radii through the body-length constant, must be equal.
+    from gravity_gb300 import ic
+
+    n = 8192
+    b = ic.uniform_merge(n, seed=6)
+    b["pos_mass"][:, :3] *= 0.05
+    b["vel_density"][:, 3] = 1.0  # stellar densities
+    b["pos_mass"][:, 3] = np.float32(1e-3)
+    year = 3.15576e7
+    ua = abi.units(mass=1.989e30, density=1.408e3, length=1.496e11, time=year)
+    g, o = make_pair(oracle_mod, BarnesHut, b, np.array([-1, -1, -1, 1, 1, 1], np.float32), units=ua)
+
+    def derived(u):
+        G = 6.67430e-11 * u.len ** -3 * u.time ** 2 * u.mass
+        blc = 0.6203504909 * (u.mass / u.density) ** (1 / 3) / u.len
+        return G, blc
+
+    def check_constants(u):
+        sg, so = g.read_sim_values(), o.read_sim_values()
+        G, blc = derived(u)
+        assert abs(sg.gravitational_constant - so.gravitational_constant) <= 3e-7 * abs(so.gravitational_constant)
+        assert abs(sg.body_length_constant - so.body_length_constant) <= 3e-7 * abs(so.body_length_constant)
+        assert abs(sg.gravitational_constant - G) <= 1e-5 * G
+        assert abs(sg.body_length_constant - blc) <= 1e-5 * blc
+        return sg.gravitational_constant
+
+    G0 = check_constants(ua)
+    assert 38.0 < G0 < 40.5  # about 4 pi^2 AU^3 / (Msun yr^2)
+    p = abi.step_params(dt=1e-4, theta=0.5, softening=1e-6, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+    keep = abi.StepParams.from_buffer_copy(p)
+    keep.units = abi.units(mass=0.0)  # mass 0: keep the current units
+    for _ in range(2):
+        g.step(keep)
+        o.step(keep)
+    assert check_constants(ua) == G0
+    # a new time unit (one month) from the next step on
+    ub = abi.units(mass=1.989e30, density=1.408e3, length=1.496e11, time=year / 12)
+    change = abi.StepParams.from_buffer_copy(p)
+    change.units = ub
+    g.step(change)
+    o.step(change)
+    G1 = check_constants(ub)
+    assert abs(G1 * 144 - G0) <= 1e-5 * G0
+    tg, to = g.read_merge_tasks(), o.read_merge_tasks()
+    assert len(to) > 0
+    assert set(map(tuple, tg.tolist())) == set(map(tuple, to.tolist()))
+    assert g.read_stats().merged == o.read_stats().merged
+    pg, po = g.read_bodies()["pos_mass"], o.read_bodies()["pos_mass"]
+    assert np.array_equal(pg[:, 3] == 0, po[:, 3] == 0)
+    np.testing.assert_allclose(pg, po, rtol=1e-5, atol=1e-6)
