@@ -74,6 +74,12 @@ def _declare(L):
         "gbh_sort_pairs_noalloc": [vp, vp, vp, vp, u32, vp],
         "gbh_exchange_bodies": [vp, vp, vp, u32, u32],
         "gbh_step_streamed": [vp, sp, vp, vp],
+        "gbh_step_shard_walk": [vp, sp, u32, u32, C.POINTER(u32)],
+        "gbh_shard_pack": [vp, u32, u32, vp],
+        "gbh_shard_unpack": [vp, u32, u32, vp],
+        "gbh_read_merge_tasks_full": [vp, vp, vp, vp, u32, C.POINTER(u32)],
+        "gbh_write_merge_tasks": [vp, vp, vp, vp, u32],
+        "gbh_step_shard_finish": [vp, u32],
         "gbh_step_streamed_finish": [vp, vp],
         "gbh_generate_bodies": [vp, C.POINTER(abi.IcParams), u64, u32, u32],
         "gbh_select_glow_nodes": [vp, C.POINTER(abi.View), vp, u32, C.POINTER(u32)],

@@ -102,6 +102,52 @@ class BarnesHut:
         self._chk(lib().gbh_step_streamed_finish(self._h, None if out is None else _ptr(out)))
         return last_result
 
+    # ---- the sharded step (gbh_step_shard_*; orchestrated by sharded.ShardedStep)
+    def step_shard_walk(self, params: abi.StepParams, rank: int, world: int) -> tuple[int, int]:
+        """Tree of the whole state and this rank's share of the walk; returns
+        the sorted slots [lo, hi) it updated."""
+        r = (C.c_uint32 * 2)()
+        self._chk(lib().gbh_step_shard_walk(self._h, C.byref(params), rank, world, r))
+        return int(r[0]), int(r[1])
+
+    def shard_pack_tensor(self, lo: int, hi: int):
+        """The updated bodies of slots [lo, hi), slot order, as a uint8 tensor
+        on this context's GPU (the all-gather's send buffer)."""
+        import torch
+
+        t = torch.empty((hi - lo) * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{self.device}")
+        self._chk(lib().gbh_shard_pack(self._h, lo, hi - lo, C.c_void_p(t.data_ptr())))
+        return t
+
+    def shard_unpack_tensor(self, lo: int, t):
+        """Install another rank's bodies of slots [lo, lo + len): a uint8 tensor
+        on this context's GPU, complete on torch's current stream."""
+        import torch
+
+        torch.cuda.current_stream(self.device).synchronize()
+        count = t.numel() // abi.BODY_DTYPE.itemsize
+        self._chk(lib().gbh_shard_unpack(self._h, lo, count, C.c_void_p(t.data_ptr())))
+
+    def read_merge_tasks_full(self):
+        cnt = C.c_uint32(0)
+        self._chk(lib().gbh_read_merge_tasks_full(self._h, None, None, None, 0, C.byref(cnt)))
+        pairs = np.zeros((cnt.value, 2), np.uint32)
+        keys = np.zeros(cnt.value, np.uint64)
+        slots = np.zeros(cnt.value, np.uint32)
+        if cnt.value:
+            self._chk(lib().gbh_read_merge_tasks_full(self._h, _ptr(pairs), _ptr(keys), _ptr(slots), cnt.value,
+                                                      C.byref(cnt)))
+        return pairs, keys, slots
+
+    def write_merge_tasks(self, pairs, keys, slots):
+        p = np.ascontiguousarray(pairs, np.uint32)
+        k = np.ascontiguousarray(keys, np.uint64)
+        s = np.ascontiguousarray(slots, np.uint32)
+        self._chk(lib().gbh_write_merge_tasks(self._h, _ptr(p), _ptr(k), _ptr(s), len(k)))
+
+    def step_shard_finish(self, out_of_bounds_other_ranks: int):
+        self._chk(lib().gbh_step_shard_finish(self._h, int(out_of_bounds_other_ranks)))
+
     def generate_bodies(self, params: abi.IcParams, seed: int = 0, count: int | None = None, offset: int = 0):
         """Seeded initial conditions written on the device (gbh_generate_bodies)."""
         count = self.n - offset if count is None else count

@@ -65,6 +65,7 @@ struct DevState {
     uint32_t fill_frontier;            // nodes handed from the tiled fill to the top-tree fill
     uint32_t sorted_valid;             // sorted_pm holds the current positions in index order
     uint32_t view_count;               // records of the last node selection (gbh_select_*)
+    uint32_t shard_lo, shard_hi;       // sorted slots a sharded walk updated [lo, hi)
     unsigned long long interactions;
     unsigned long long opened;
     unsigned long long mac_evals;
@@ -133,7 +134,17 @@ struct StepBuffers {
     uint32_t sort_tiles_cap;
     uint32_t prep_tiles_cap;
     uint32_t num_sms;  // multiprocessors of the context's device (grid sizes of the persistent kernels)
+    // sharded walk: this rank's share of the live bodies (world 1: all)
+    uint32_t shard_rank, shard_world;
 };
+
+// The walk's share of rank r of W: sorted slots [n r / W, n (r + 1) / W).  The
+// plain walk updates exactly these slots; the group walks walk the groups
+// whose first slot lies in them.
+__device__ __forceinline__ void shard_slots(const StepBuffers& b, uint32_t n, uint32_t& lo, uint32_t& hi) {
+    lo = (uint32_t)((uint64_t)n * b.shard_rank / b.shard_world);
+    hi = (uint32_t)((uint64_t)n * (b.shard_rank + 1) / b.shard_world);
+}
 
 // ---- GLSL built-in semantics (GLSL 4.30 §8.3) -------------------------------
 __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
@@ -322,4 +333,10 @@ void launch_direct_sum64(const double* pos64, const gbh_body* bodies, uint32_t n
 void launch_diagnostics(const gbh_body* bodies, uint32_t nb, const double* pos64, const float* potential,
                         double* partial, uint32_t blocks, double* out, cudaStream_t s);
 void launch_merge(const StepBuffers& b, cudaStream_t s);
+// sharded walk: the updated slot range into st->shard_lo/hi (after the walk),
+// and the copies of updated bodies out of and into the output body buffer
+void launch_shard_range(const StepBuffers& b, bool groups, cudaStream_t s);
+void launch_shard_pack(const StepBuffers& b, uint32_t lo, uint32_t count, gbh_body* out, cudaStream_t s);
+void launch_shard_unpack(const StepBuffers& b, uint32_t lo, uint32_t count, const gbh_body* in, cudaStream_t s);
+void launch_shard_add_oob(const StepBuffers& b, uint32_t oob, cudaStream_t s);
 void launch_init_index(uint32_t* idx, uint32_t N, gbh_sim_values* sim, const gbh_units* units_dev, cudaStream_t s);

@@ -101,6 +101,8 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.sort_tiles_cap = c->sort_tiles_cap;
     b.prep_tiles_cap = c->prep_tiles_cap;
     b.num_sms = c->num_sms;
+    b.shard_rank = c->shard_rank;
+    b.shard_world = c->shard_world;
     return b;
 }
 
@@ -513,6 +515,113 @@ int gbh_step_streamed_finish(gbh_ctx* c, gbh_body* last_result) {
     return gbh_synchronize(c);
 }
 
+// ---- sharded step -------------------------------------------------------------
+
+static int read_dev(gbh_ctx* c, void* host, const void* dev, size_t bytes);
+
+int gbh_step_shard_walk(gbh_ctx* c, const gbh_step_params* p, uint32_t rank, uint32_t world, uint32_t range[2]) {
+    if (!c || !p || !range) return fail(c, GBH_ERR_INVALID, "null argument");
+    if (!c->inited) return fail(c, GBH_ERR_STATE, "gbh_step_shard_walk before gbh_init");
+    if (c->shard_open) return fail(c, GBH_ERR_STATE, "a sharded step is already open");
+    if (world == 0 || rank >= world) return fail(c, GBH_ERR_INVALID, "rank must be below world");
+    if (p->precision_mode != GBH_PRECISION_FP32)
+        return fail(c, GBH_ERR_UNSUPPORTED, "the sharded step runs the FP32 form");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    int rc = upload_params(c, p);
+    if (rc) return rc;
+    // the tree of the whole state, as every rank builds it
+    if ((rc = enqueue_reset(c)) || (rc = enqueue_prepare(c)) || (rc = enqueue_sort(c)) || (rc = enqueue_build(c)) ||
+        (rc = enqueue_fill(c)))
+        return rc;
+    // this rank's share of the walk and the slots it updated
+    c->shard_rank = rank;
+    c->shard_world = world;
+    rc = enqueue_walk(c);
+    if (!rc) {
+        launch_shard_range(ctx_buffers(c), c->mac_mode != GBH_MAC_PLAIN, c->stream);
+        rc = check_launch(c, "shard range");
+    }
+    c->shard_rank = 0;
+    c->shard_world = 1;
+    if (rc) return rc;
+    c->shard_open = true;
+    if ((rc = gbh_synchronize(c))) return rc;
+    uint32_t r[2];
+    CUDA_TRY(c, cudaMemcpy(r, &c->st->shard_lo, 8, cudaMemcpyDeviceToHost));
+    range[0] = r[0];
+    range[1] = r[1];
+    return GBH_OK;
+}
+
+int gbh_shard_pack(gbh_ctx* c, uint32_t lo, uint32_t count, void* device_out) {
+    if (!c || (!device_out && count)) return fail(c, GBH_ERR_INVALID, "null argument");
+    if (!c->shard_open) return fail(c, GBH_ERR_STATE, "no sharded step is open");
+    if ((uint64_t)lo + count > c->N) return fail(c, GBH_ERR_INVALID, "slot range exceeds initial_num_bodies");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_shard_pack(ctx_buffers(c), lo, count, static_cast<gbh_body*>(device_out), c->stream);
+    int rc = check_launch(c, "shard pack");
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_shard_unpack(gbh_ctx* c, uint32_t lo, uint32_t count, const void* device_in) {
+    if (!c || (!device_in && count)) return fail(c, GBH_ERR_INVALID, "null argument");
+    if (!c->shard_open) return fail(c, GBH_ERR_STATE, "no sharded step is open");
+    if ((uint64_t)lo + count > c->N) return fail(c, GBH_ERR_INVALID, "slot range exceeds initial_num_bodies");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_shard_unpack(ctx_buffers(c), lo, count, static_cast<const gbh_body*>(device_in), c->stream);
+    int rc = check_launch(c, "shard unpack");
+    if (rc) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_read_merge_tasks_full(gbh_ctx* c, uint32_t* pairs, uint64_t* keys, uint32_t* slots, uint32_t capacity,
+                              uint32_t* count) {
+    if (!c || !count) return GBH_ERR_INVALID;
+    uint32_t ht[2];
+    int rc = read_dev(c, ht, c->mq, 8);
+    if (rc) return rc;
+    const uint32_t m = ht[1] < c->N ? ht[1] : c->N;
+    *count = m;
+    const uint32_t k = m < capacity ? m : capacity;
+    if (!k) return GBH_OK;
+    if (pairs && (rc = read_dev(c, pairs, c->mq->pairs, (size_t)k * 8))) return rc;
+    if (keys && (rc = read_dev(c, keys, c->mkeys, (size_t)k * 8))) return rc;
+    if (slots && (rc = read_dev(c, slots, c->mslots, (size_t)k * 4))) return rc;
+    return GBH_OK;
+}
+
+int gbh_write_merge_tasks(gbh_ctx* c, const uint32_t* pairs, const uint64_t* keys, const uint32_t* slots,
+                          uint32_t count) {
+    if (!c || (count && (!pairs || !keys || !slots))) return fail(c, GBH_ERR_INVALID, "null argument");
+    if (count > c->N) return fail(c, GBH_ERR_INVALID, "more merge tasks than bodies");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const uint32_t ht[2] = {0u, count};
+    CUDA_TRY(c, cudaMemcpyAsync(c->mq, ht, 8, cudaMemcpyHostToDevice, c->stream));
+    if (count) {
+        CUDA_TRY(c, cudaMemcpyAsync(c->mq->pairs, pairs, (size_t)count * 8, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->mkeys, keys, (size_t)count * 8, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(c->mslots, slots, (size_t)count * 4, cudaMemcpyHostToDevice, c->stream));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return GBH_OK;
+}
+
+int gbh_step_shard_finish(gbh_ctx* c, uint32_t out_of_bounds_other_ranks) {
+    if (!c) return GBH_ERR_INVALID;
+    if (!c->shard_open) return fail(c, GBH_ERR_STATE, "no sharded step is open");
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    launch_shard_add_oob(ctx_buffers(c), out_of_bounds_other_ranks, c->stream);
+    int rc = check_launch(c, "shard out-of-bounds count");
+    if (rc) return rc;
+    if ((rc = enqueue_merge(c)) || (rc = enqueue_swap(c))) return rc;
+    after_swap(c, false);
+    c->shard_open = false;
+    return gbh_synchronize(c);
+}
+
 int gbh_generate_bodies(gbh_ctx* c, const gbh_ic_params* p, uint64_t seed, uint32_t count, uint32_t offset) {
     if (!c || !p) return fail(c, GBH_ERR_INVALID, "null argument");
     if ((uint64_t)offset + count > c->N) return fail(c, GBH_ERR_INVALID, "generate range exceeds initial_num_bodies");
@@ -555,6 +664,7 @@ int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1);
 int gbh_step_n(gbh_ctx* c, const gbh_step_params* p, uint32_t count) {
     if (!c) return fail(c, GBH_ERR_INVALID, "null context");
     if (!c->inited) return fail(c, GBH_ERR_STATE, "gbh_step before gbh_init");
+    if (c->shard_open) return fail(c, GBH_ERR_STATE, "a sharded step is open: gbh_step_shard_finish first");
     CUDA_TRY(c, cudaSetDevice(c->device));
     int rc = upload_params(c, p);
     if (rc) return rc;

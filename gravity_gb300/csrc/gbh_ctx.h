@@ -85,6 +85,10 @@ struct gbh_ctx {
     cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_done = nullptr;
     bool stream_have_result = false;  // stage_out holds the result of the last streamed step
 
+    // sharded step (gbh_step_shard_walk ... gbh_step_shard_finish)
+    uint32_t shard_rank = 0, shard_world = 1;  // the walk's share while a shard walk is enqueued
+    bool shard_open = false;                   // a shard walk ran; finish it before the next step
+
     std::map<int, cudaGraphExec_t> graphs;
     std::string last_error;
 };

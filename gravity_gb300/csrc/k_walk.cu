@@ -51,7 +51,10 @@ __global__ __launch_bounds__(WALK_THREADS) void k_walk_plain(StepBuffers b) {
     const uint32_t g = warp_global * 32 + lane;
     if (blockIdx.x == 0 && threadIdx.x == 0) b.st->sorted_valid = 1u;  // the update below fills sorted_pm
     if (warp_global * 32 >= n) return;
-    const bool active = g < n;
+    uint32_t s_lo, s_hi;
+    shard_slots(b, n, s_lo, s_hi);
+    if (warp_global * 32 + 32 <= s_lo || warp_global * 32 >= s_hi) return;
+    const bool active = g < n && g >= s_lo && g < s_hi;
     const gbh_step_params* P = b.params;
     const gbh_sim_values* sim = b.sim;
     const float G = sim->gravitational_constant;

@@ -168,6 +168,12 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
     if (lane == 0) gi = atomicAdd(&b.st->group_next, 1u);
     gi = __shfl_sync(0xffffffffu, gi, 0);
     if (gi >= num_groups) break;
+    if (b.shard_world > 1) {  // a sharded walk: this rank's groups only
+        uint32_t s_lo, s_hi;
+        shard_slots(b, n, s_lo, s_hi);
+        const uint32_t first = b.groups[gi].x;
+        if (first < s_lo || first >= s_hi) continue;
+    }
     const uint2 grp = b.groups[gi];
     uint32_t gq[GW_BPL];
     bool actq[GW_BPL];

@@ -257,6 +257,38 @@ int gbh_step_n(gbh_ctx* ctx, const gbh_step_params* params, uint32_t count);
 int gbh_synchronize(gbh_ctx* ctx);
 int gbh_clear_error(gbh_ctx* ctx);
 
+/* ---- sharded step (one process per GPU; the exchange is the caller's) ------
+ * One BarnesHut.step split over `world` ranks.  Every rank holds the whole
+ * state and builds the whole tree (the stages before the walk are
+ * deterministic, so all ranks build the same one); each walks only its share
+ * of the live bodies, sorted slots [n r / W, n (r + 1) / W) (the group walks:
+ * the groups whose first slot lies there).  The reference walks every body
+ * independently of the others (bh_force.comp:40-142), so the split walk
+ * equals the whole walk body for body.  Per step, on every rank:
+ *   1. gbh_step_shard_walk: reset, compaction, sort, build, fill and this
+ *      rank's walk; range = the sorted slots [lo, hi) it updated (the ranks'
+ *      ranges tile [0, n) in rank order);
+ *   2. gbh_shard_pack: its updated bodies, slot order, into a DEVICE buffer;
+ *   3. the caller all-gathers the ranges and packed bodies (NCCL, or any
+ *      transport), and gbh_shard_unpack installs every other rank's range;
+ *   4. gbh_read_merge_tasks_full / gbh_write_merge_tasks: the caller gathers
+ *      every rank's merge tasks and writes the union (any order) on every rank;
+ *   5. gbh_step_shard_finish: adds the other ranks' out-of-bounds kills to
+ *      SimulationValues.outOfBounds, resolves the merges and swaps.
+ * The state is then the same on every rank and equal, bit for bit, to one
+ * gbh_step on one rank.  FP32 form only (GBH_ERR_UNSUPPORTED otherwise). */
+int gbh_step_shard_walk(gbh_ctx* ctx, const gbh_step_params* params, uint32_t rank, uint32_t world,
+                        uint32_t range[2]);
+int gbh_shard_pack(gbh_ctx* ctx, uint32_t lo, uint32_t count, void* device_out);
+int gbh_shard_unpack(gbh_ctx* ctx, uint32_t lo, uint32_t count, const void* device_in);
+/* the last walk's merge tasks: pairs (body, other), ordering keys (sorted slot
+ * << 32 | sequence) and the sorted slot of each task's second body */
+int gbh_read_merge_tasks_full(gbh_ctx* ctx, uint32_t* pairs, uint64_t* keys, uint32_t* slots, uint32_t capacity,
+                              uint32_t* count);
+int gbh_write_merge_tasks(gbh_ctx* ctx, const uint32_t* pairs, const uint64_t* keys, const uint32_t* slots,
+                          uint32_t count);
+int gbh_step_shard_finish(gbh_ctx* ctx, uint32_t out_of_bounds_other_ranks);
+
 /* ---- read-back (synchronous; host buffers are caller-owned) --------------- */
 #define GBH_BODIES_IN 0u
 #define GBH_BODIES_OUT 1u

@@ -783,8 +783,8 @@ static int cmp_u64_pair(const void* a, const void* b) {
     return x < y ? -1 : (x > y ? 1 : 0);
 }
 
-int orc_stage_walk(orc_ctx* c, const gbh_step_params* p) {
-    const uint32_t n = c->sim.num_bodies;
+/* the walk of sorted slots [lo, hi) */
+static int walk_slots(orc_ctx* c, const gbh_step_params* p, uint32_t lo, uint32_t hi) {
     gbh_body* dst = c->bodies[1 - c->bin];
     c->store_accel = (p->flags & GBH_FLAG_STORE_ACCEL) != 0;
     uint64_t opened = 0, inter = 0;
@@ -802,7 +802,7 @@ int orc_stage_walk(orc_ctx* c, const gbh_step_params* p) {
         uint32_t* stack = (uint32_t*)malloc(sizeof(uint32_t) * stack_cap);
         walk_counts wc = {0, 0, 0};
 #pragma omp for schedule(dynamic, 256)
-        for (int64_t g = 0; g < (int64_t)n; ++g) walk_body(c, p, (uint32_t)g, dst, &tbs[t], &wc, stack, stack_cap);
+        for (int64_t g = lo; g < (int64_t)hi; ++g) walk_body(c, p, (uint32_t)g, dst, &tbs[t], &wc, stack, stack_cap);
         opened += wc.opened;
         inter += wc.interactions;
         oob += wc.oob;
@@ -838,6 +838,71 @@ int orc_stage_walk(orc_ctx* c, const gbh_step_params* p) {
     c->oob_step += oob;
     c->sim.out_of_bounds += oob;
     c->sim.uint_debug[0] += (uint32_t)opened;
+    return GBH_OK;
+}
+
+int orc_stage_walk(orc_ctx* c, const gbh_step_params* p) { return walk_slots(c, p, 0, c->sim.num_bodies); }
+
+/* ---- the sharded step (the GPU's gbh_step_shard_* restated): rank r of W
+ * walks sorted slots [n r / W, n (r + 1) / W); bh_force.comp:40-142 walks
+ * every body independently, so the shares together equal the whole walk. */
+int orc_step_shard_walk(orc_ctx* c, const gbh_step_params* p, uint32_t rank, uint32_t world, uint32_t range[2]) {
+    if (!c || !p || !range || world == 0 || rank >= world) return GBH_ERR_INVALID;
+    orc_stage_reset(c, p);
+    orc_stage_partition(c);
+    orc_stage_decrement(c);
+    if (p->static_or_dynamic == GBH_BOUNDS_DYNAMIC) orc_stage_bounds(c);
+    orc_stage_encode(c);
+    int rc = orc_stage_sort(c);
+    if (rc) return rc;
+    orc_stage_build(c);
+    if ((rc = orc_stage_fill(c))) return rc;
+    const uint64_t n = c->sim.num_bodies;
+    range[0] = (uint32_t)(n * rank / world);
+    range[1] = (uint32_t)(n * (rank + 1) / world);
+    return walk_slots(c, p, range[0], range[1]);
+}
+
+int orc_shard_pack(orc_ctx* c, uint32_t lo, uint32_t count, gbh_body* out) {
+    if (!c || (!out && count) || (uint64_t)lo + count > c->N) return GBH_ERR_INVALID;
+    const gbh_body* dst = c->bodies[1 - c->bin];
+    const uint32_t* in = c->index[c->iin];
+    for (uint32_t i = 0; i < count; ++i) out[i] = dst[in[lo + i]];
+    return GBH_OK;
+}
+
+int orc_shard_unpack(orc_ctx* c, uint32_t lo, uint32_t count, const gbh_body* body) {
+    if (!c || (!body && count) || (uint64_t)lo + count > c->N) return GBH_ERR_INVALID;
+    gbh_body* dst = c->bodies[1 - c->bin];
+    const uint32_t* in = c->index[c->iin];
+    for (uint32_t i = 0; i < count; ++i) dst[in[lo + i]] = body[i];
+    return GBH_OK;
+}
+
+int orc_read_merge_tasks_full(orc_ctx* c, uint32_t* pairs, uint64_t* keys, uint32_t capacity, uint32_t* count) {
+    if (!c || !count) return GBH_ERR_INVALID;
+    *count = c->mtail;
+    const uint32_t k = c->mtail < capacity ? c->mtail : capacity;
+    if (pairs) memcpy(pairs, c->mtasks, (size_t)k * 8);
+    if (keys) memcpy(keys, c->mkeys, (size_t)k * 8);
+    return GBH_OK;
+}
+
+/* tasks in ascending key order: the merge applies them in array order */
+int orc_write_merge_tasks(orc_ctx* c, const uint32_t* pairs, const uint64_t* keys, uint32_t count) {
+    if (!c || (count && (!pairs || !keys)) || count > c->mcap) return GBH_ERR_INVALID;
+    memcpy(c->mtasks, pairs, (size_t)count * 8);
+    memcpy(c->mkeys, keys, (size_t)count * 8);
+    c->mtail = count;
+    return GBH_OK;
+}
+
+int orc_step_shard_finish(orc_ctx* c, uint32_t oob_other_ranks) {
+    if (!c) return GBH_ERR_INVALID;
+    c->sim.out_of_bounds += oob_other_ranks;
+    c->oob_step += oob_other_ranks;
+    orc_stage_merge(c);
+    orc_stage_swap(c);
     return GBH_OK;
 }
 

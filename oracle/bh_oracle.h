@@ -55,6 +55,13 @@ int orc_stage_swap(orc_ctx* c);                                 /* GPU.swapBodyB
 /* the walk over every `stride`-th live sorted slot only (CPU-baseline samples);
  * writes nothing to the body buffers */
 int orc_stage_walk_sample(orc_ctx* c, const gbh_step_params* p, uint32_t stride, uint64_t* interactions);
+/* the sharded step (gbh_step_shard_* of the C ABI, restated) */
+int orc_step_shard_walk(orc_ctx* c, const gbh_step_params* p, uint32_t rank, uint32_t world, uint32_t range[2]);
+int orc_shard_pack(orc_ctx* c, uint32_t lo, uint32_t count, gbh_body* out);
+int orc_shard_unpack(orc_ctx* c, uint32_t lo, uint32_t count, const gbh_body* body);
+int orc_read_merge_tasks_full(orc_ctx* c, uint32_t* pairs, uint64_t* keys, uint32_t capacity, uint32_t* count);
+int orc_write_merge_tasks(orc_ctx* c, const uint32_t* pairs, const uint64_t* keys, uint32_t count);
+int orc_step_shard_finish(orc_ctx* c, uint32_t oob_other_ranks);
 
 int orc_read_bodies(orc_ctx* c, uint32_t which, gbh_body* host, uint32_t count, uint32_t offset);
 int orc_read_leaf_nodes(orc_ctx* c, gbh_node* host, uint32_t count, uint32_t offset);

@@ -72,6 +72,12 @@ def lib():
             "orc_write_index": [vp, vp, u32, u32],
             "orc_write_morton": [vp, vp, u32, u32],
             "orc_direct_sum_fp64": [vp, u32, vp, u32, C.c_double, C.c_double, vp],
+            "orc_step_shard_walk": [vp, sp, u32, u32, C.POINTER(u32)],
+            "orc_shard_pack": [vp, u32, u32, vp],
+            "orc_shard_unpack": [vp, u32, u32, vp],
+            "orc_read_merge_tasks_full": [vp, vp, vp, u32, C.POINTER(u32)],
+            "orc_write_merge_tasks": [vp, vp, vp, u32],
+            "orc_step_shard_finish": [vp, u32],
             "orc_safe_lcp": [vp, i32, i32, i32],
         }.items():
             f = getattr(L, name)
@@ -189,6 +195,41 @@ class OracleBarnesHut:
         inter = C.c_uint64(0)
         _check(lib().orc_stage_walk_sample(self._h, C.byref(p), stride, C.byref(inter)), "walk_sample")
         return int(inter.value)
+
+    # the sharded step (same method names as gravity_gb300.BarnesHut)
+    def step_shard_walk(self, p, rank: int, world: int) -> tuple[int, int]:
+        r = (C.c_uint32 * 2)()
+        _check(lib().orc_step_shard_walk(self._h, C.byref(p), rank, world, r), "step_shard_walk")
+        return int(r[0]), int(r[1])
+
+    def shard_pack_tensor(self, lo: int, hi: int):
+        import torch
+
+        out = np.zeros(hi - lo, dtype=abi.BODY_DTYPE)
+        _check(lib().orc_shard_pack(self._h, lo, hi - lo, _ptr(out)), "shard_pack")
+        return torch.from_numpy(out.view(np.uint8).copy())
+
+    def shard_unpack_tensor(self, lo: int, t):
+        a = np.ascontiguousarray(t.cpu().numpy()).view(abi.BODY_DTYPE)
+        _check(lib().orc_shard_unpack(self._h, lo, len(a), _ptr(a)), "shard_unpack")
+
+    def read_merge_tasks_full(self):
+        cnt = C.c_uint32(0)
+        _check(lib().orc_read_merge_tasks_full(self._h, None, None, 0, C.byref(cnt)), "read_merge_tasks_full")
+        pairs = np.zeros((cnt.value, 2), np.uint32)
+        keys = np.zeros(cnt.value, np.uint64)
+        if cnt.value:
+            _check(lib().orc_read_merge_tasks_full(self._h, _ptr(pairs), _ptr(keys), cnt.value, C.byref(cnt)),
+                   "read_merge_tasks_full")
+        return pairs, keys, np.zeros(cnt.value, np.uint32)
+
+    def write_merge_tasks(self, pairs, keys, slots):
+        p = np.ascontiguousarray(pairs, np.uint32)
+        k = np.ascontiguousarray(keys, np.uint64)
+        _check(lib().orc_write_merge_tasks(self._h, _ptr(p), _ptr(k), len(k)), "write_merge_tasks")
+
+    def step_shard_finish(self, out_of_bounds_other_ranks: int):
+        _check(lib().orc_step_shard_finish(self._h, out_of_bounds_other_ranks), "step_shard_finish")
 
     # read-back
     def read_bodies(self, which=abi.BODIES_IN, count=None, offset=0) -> np.ndarray:
