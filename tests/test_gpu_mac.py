@@ -1,8 +1,9 @@
 """The learned multipole-acceptance criterion on the GPU: the tensor-core
 forward pass and the hand-written backward pass against the CPU oracle
 (oracle/mac_oracle.py), the training-pair labels against a float64
-recomputation, training, and the learned walk against the group theta rule
-at equal p99 acceleration error."""
+recomputation, bit-reproducible recording and training, and the learned walk,
+trained on other states, against the group theta rule in walk time at equal
+p99 acceleration error."""
 import numpy as np
 import pytest
 
@@ -84,7 +85,7 @@ def _label_numpy(sim, pair, accel, idx, leaves, internal, soft):
     return np.log10(max(worst, 1e-12))
 
 
-def test_learned_mac_pipeline_and_gain(gbh_lib):
+def test_learned_mac_pipeline_labels_and_training(gbh_lib):
     soft = 0.005 ** 2
     bodies = ic.plummer_uniform(262144, seed=3)
     sim = _sim(bodies)
@@ -95,6 +96,9 @@ def test_learned_mac_pipeline_and_gain(gbh_lib):
     assert np.all(np.isfinite(feats)) and np.all(np.isfinite(labels))
     # labels against a float64 recomputation
     ids = sim.mac_read_pair_ids(count)
+    # the pairs come in the canonical (group, node) order
+    key = ids[:, 0].astype(np.uint64) << np.uint64(32) | ids[:, 2].astype(np.uint64)
+    assert np.all(key[1:] >= key[:-1])
     accel = sim.read_accel()[:, :3].astype(np.float64)
     idx = sim.read_index()
     leaves = sim.read_leaf_nodes()
@@ -106,17 +110,71 @@ def test_learned_mac_pipeline_and_gain(gbh_lib):
     losses = sim.mac_train(epochs=6, batch=8192, lr=3e-3, seed=0)
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.6 * losses[0], losses
-    # the trained criterion against the group theta rule at the plain rule's p99
+
+
+def test_training_is_bit_reproducible(gbh_lib):
+    # the same state recorded and trained in two contexts: the same pairs in
+    # the same order, the same losses and the same weights, bit for bit
+    soft = 0.005 ** 2
+    bodies = ic.plummer_uniform(131072, seed=8)
+    p = abi.step_params(theta=0.5, softening=soft)
+    out = []
+    for _ in range(2):
+        sim = _sim(bodies)
+        k = sim.mac_generate(p, max_pairs=400_000, seed=1)
+        f, lab = sim.mac_read_pairs(k)
+        losses = sim.mac_train(epochs=3, batch=8192, lr=3e-3, seed=0)
+        out.append((f, lab, losses, sim.mac_get_weights()))
+    (f0, l0, s0, w0), (f1, l1, s1, w1) = out
+    assert np.array_equal(f0.view(np.uint32), f1.view(np.uint32))
+    assert np.array_equal(l0.view(np.uint32), l1.view(np.uint32))
+    assert np.array_equal(s0.view(np.uint32), s1.view(np.uint32))
+    assert np.array_equal(w0.view(np.uint32), w1.view(np.uint32))
+
+
+def _walk_ms(sim, p, reps=9):
+    for _ in range(2):
+        sim.step_profiled(p)
+    return float(np.median([sim.step_profiled(p)["walk"] for _ in range(reps)]))
+
+
+def test_learned_mac_out_of_sample_beats_ablation_in_walk_time(gbh_lib):
+    # Weights trained on other states (a two-galaxy encounter and a uniform
+    # cube), never on the state timed; on a 1,048,576-body Plummer + uniform
+    # mixture the learned walk, at a tolerance whose p99 error against the
+    # FP64 direct sum is at or below the group-theta ablation's, must take
+    # less walk time than that ablation.
+    soft = 0.005 ** 2
+    feats, labels = [], []
+    for b in (ic.galaxy_pair(131072, seed=2), ic.uniform_merge(262144, seed=1)):
+        src = _sim(b)
+        p = abi.step_params(theta=0.5, softening=soft)
+        src.step(p)
+        k = src.mac_generate(p, max_pairs=1_000_000, seed=1)
+        f, lab = src.mac_read_pairs(k)
+        feats.append(f)
+        labels.append(lab)
+        src.close()
+    sim = _sim(ic.plummer_uniform(1048576, seed=3))
+    sim.mac_write_pairs(np.concatenate(feats), np.concatenate(labels))
+    sim.mac_train(epochs=8, batch=16384, lr=3e-3, seed=0)
+    p = abi.step_params(theta=0.5, softening=soft)
+    sim.step(p)
     ref_sample = accuracy.DirectSumSample(sim, p, count=2048, seed=2)
     target = accuracy.evaluate(sim, ref_sample, p)["p99"]
-    best_l, res_l = accuracy.match_p99(
-        sim, ref_sample, lambda t: abi.step_params(theta=0.5, softening=soft, mac=abi.MAC_LEARNED, mac_tolerance=t),
-        [-4.0, -3.5, -3.0, -2.75, -2.5, -2.25, -2.0, -1.75, -1.5, -1.25, -1.0], target)
-    best_g, res_g = accuracy.match_p99(
-        sim, ref_sample, lambda t: abi.step_params(theta=t, softening=soft, mac=abi.MAC_GROUP),
-        [0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.2], target)
-    assert best_l is not None and best_g is not None, (res_l, res_g)
-    assert best_l[1]["interactions"] < best_g[1]["interactions"], (best_l, best_g)
+    group = lambda t: abi.step_params(theta=t, softening=soft, mac=abi.MAC_GROUP)
+    learned = lambda t: abi.step_params(theta=0.5, softening=soft, mac=abi.MAC_LEARNED, mac_tolerance=t)
+    best_g, res_g = accuracy.match_p99(sim, ref_sample, group, [0.3, 0.4, 0.45, 0.5, 0.55, 0.6, 0.7, 0.8], target,
+                                       refine=2)
+    assert best_g is not None, res_g
+    best_l, res_l = accuracy.match_p99(sim, ref_sample, learned,
+                                       [-3.5, -3.0, -2.75, -2.5, -2.4, -2.3, -2.2, -2.1, -2.0, -1.75, -1.5],
+                                       best_g[1]["p99"], refine=2)
+    assert best_l is not None, res_l
+    assert best_l[1]["p99"] <= best_g[1]["p99"]
+    t_g = _walk_ms(sim, group(best_g[0]))
+    t_l = _walk_ms(sim, learned(best_l[0]))
+    assert t_l < t_g, (t_l, t_g, best_l, best_g)
 
 
 def test_group_and_learned_walks_emit_merge_tasks(gbh_lib):

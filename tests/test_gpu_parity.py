@@ -336,7 +336,10 @@ def test_derived_units_and_mid_run_update(gbh_lib, oracle_mod):
         G, blc = derived(u)
         assert abs(sg.gravitational_constant - so.gravitational_constant) <= 3e-7 * abs(so.gravitational_constant)
         assert abs(sg.body_length_constant - so.body_length_constant) <= 3e-7 * abs(so.body_length_constant)
-        assert abs(sg.gravitational_constant - G) <= 1e-5 * G
+        # the reference's FP32 order (6.6743e-11 * len^-3 first) passes through
+        # a subnormal, about 2e-44, for these units, so its G is 1.6% from the
+        # exact value; both sides keep that order
+        assert abs(sg.gravitational_constant - G) <= 0.05 * G
         assert abs(sg.body_length_constant - blc) <= 1e-5 * blc
         return sg.gravitational_constant
 
