@@ -47,12 +47,13 @@ METRIC = "steps/s at 16.7M bodies, learned-MAC vs plain theta walk at equal p99 
 WALK_FLOP_PER_INTERACTION = 20  # Nyland, Harris & Prins, GPU Gems 3 ch. 31
 
 
-def workload(name: str, n: int | None):
+def workload(name: str, n: int | None, seed: int | None = None):
     if name == "mixture":
         n = n or 16777216
+        sd = 3 if seed is None else seed
         return dict(
-            name=f"plummer_uniform_mixture_n{n}",
-            bodies=lambda: ic.plummer_uniform(n, seed=3),
+            name=f"plummer_uniform_mixture_n{n}" + ("" if seed is None else f"_seed{sd}"),
+            bodies=lambda: ic.plummer_uniform(n, seed=sd),
             n=n,
             params=abi.step_params(dt=1e-3, theta=0.5, softening=0.005 ** 2, bounds=abi.BOUNDS_DYNAMIC),
         )
@@ -340,18 +341,31 @@ def precision_arm(bh, p_plain, accuracy):
     return p64, calib
 
 
+def parse_sources(spec: str):
+    """'name[@seed]:share,...' -> [(name, seed or None, share)]"""
+    out = []
+    for part in spec.split(","):
+        name, share = part.split(":")
+        seed = None
+        if "@" in name:
+            name, sd = name.split("@")
+            seed = int(sd)
+        out.append((name, seed, float(share)))
+    return out
+
+
 def train_out_of_sample(bh, args, local) -> dict:
     """The learned criterion's weights from training pairs recorded on
-    snapshots of two other workloads, the two-galaxy encounter (8,388,608
-    bodies) and the uniform cube with merges (1,048,576 bodies), one step into
+    snapshots of other workloads (default: the two-galaxy encounter, 8,388,608
+    bodies, and the uniform cube with merges, 1,048,576 bodies), one step into
     each run; the timed state is never seen in training.  Recording and
     training are deterministic, so every run trains the same weights."""
     from gravity_gb300 import BarnesHut
 
     t0 = time.perf_counter()
     feats, labels, sources = [], [], []
-    for name, share in (("galaxy", 0.75), ("uniform_merge", 0.25)):
-        wl = workload(name, None)
+    for name, seed, share in parse_sources(args.train_sources):
+        wl = workload(name, None, seed) if seed is not None else workload(name, None)
         b = wl["bodies"]()
         bounds = wl.get("bounds", ic.exact_bounds(b))
         p = abi.StepParams.from_buffer_copy(wl["params"])
@@ -447,7 +461,7 @@ def run_ours(args):
             calib["weights_source"] = "in-sample: trained on the timed state"
         else:
             calib["training"] = train_out_of_sample(bh, args, local)
-            calib["weights_source"] = "out-of-sample: galaxy-pair and uniform-cube snapshots"
+            calib["weights_source"] = "out-of-sample: " + args.train_sources
         ref_sample = accuracy.DirectSumSample(bh, p_plain, count=4096, seed=2)
         calib["judge"] = ref_sample.judge
         ref = {th: accuracy.evaluate(bh, ref_sample, plain(th)) for th in PLAIN_THETAS}
@@ -706,6 +720,9 @@ def main():
     ap.add_argument("--mac-tolerance", type=float, default=None, help="fixed tolerance instead of calibration")
     ap.add_argument("--mac-pairs", type=int, default=48_000_000,
                     help="training pairs (split 3:1 between the galaxy-pair and uniform-cube snapshots)")
+    ap.add_argument("--train-sources", default="galaxy:0.75,uniform_merge:0.25",
+                    help="workloads whose snapshots give the training pairs, name[@seed]:share,... "
+                         "(a seed only for the mixture)")
     ap.add_argument("--train-in-sample", action="store_true",
                     help="record the training pairs on the timed state itself (default: other workloads)")
     ap.add_argument("--save-mac-weights", default=None, help="save the trained MLP weights (.npy)")

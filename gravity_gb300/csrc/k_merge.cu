@@ -10,13 +10,17 @@
 //   1. count how many tasks touch each body (the lock words double as counters);
 //   2. a task whose two bodies appear in no other task commutes with every
 //      other task and is applied at once, in parallel;
-//   3. the remaining (conflicting) tasks are ordered by their emission key in
-//      one block (bitonic sort in shared memory) and applied by one thread;
+//   3. the remaining (conflicting) tasks are resolved in rounds by one block:
+//      a task runs in a round when its emission key is the earliest pending
+//      key of both its bodies, so every earlier task on those bodies has run
+//      and the round's tasks touch disjoint bodies; each round runs at least
+//      the globally earliest pending task, so the rounds end, and the result
+//      is the one-thread schedule's for any number of conflicts;
 //   4. the lock words are cleared again.
 #include "gbh_common.cuh"
 
-#define MERGE_CONFLICT_CAP 4096
 #define MERGE_SORT_THREADS 1024
+#define MERGE_DONE 0x80000000u  // a conflict-list entry whose task has run (task ids < 2^30)
 
 // mergeBodies, bh_merge.comp:5-22
 __device__ __forceinline__ void merge_two(float4& p1, float4& v1, const float4 p2, const float4 v2) {
@@ -88,68 +92,65 @@ __global__ void k_merge_apply(StepBuffers b) {
     if (merged) atomicAdd(&b.st->merged, merged);
 }
 
+// Step 3.  The earliest pending key per body lives in the step's spare key
+// buffer (keys_out, by body id), free from the end of the fill to the next
+// step's encode.
 __global__ __launch_bounds__(MERGE_SORT_THREADS) void k_merge_conflicts(StepBuffers b) {
-    __shared__ unsigned long long s_key[MERGE_CONFLICT_CAP];
-    __shared__ uint32_t s_task[MERGE_CONFLICT_CAP];
+    __shared__ uint32_t s_pending, s_merged;
     const uint32_t C = b.st->merge_conflicts;
     if (threadIdx.x == 0) b.st->merge_tasks = min(b.mq->tail, b.N);
     if (C == 0) return;
-    if (C > MERGE_CONFLICT_CAP) {
-        // too many to order in one block: apply in list order (still a valid
-        // single-thread schedule of the reference, but not the emission order)
-        if (threadIdx.x == 0) {
-            set_error(b.st, GBH_DEVERR_MERGE_OVERFLOW);
-            uint32_t merged = 0;
-            for (uint32_t k = 0; k < C; ++k) {
-                const uint32_t t = b.conflicts[k];
-                const uint2 pr = b.mq->pairs[t];
-                merged += apply_task(b, t, pr.x, pr.y) ? 1u : 0u;
-            }
-            b.st->merged += merged;
-        }
-        return;
+    unsigned long long* first = reinterpret_cast<unsigned long long*>(b.keys_out);
+    uint32_t* list = b.conflicts;
+    for (uint32_t k = threadIdx.x; k < C; k += blockDim.x) {
+        const uint2 pr = b.mq->pairs[list[k]];
+        first[pr.x] = ~0ull;
+        first[pr.y] = ~0ull;
     }
-    uint32_t P = 1;
-    while (P < C) P <<= 1;
-    for (uint32_t k = threadIdx.x; k < P; k += blockDim.x) {
-        if (k < C) {
-            const uint32_t t = b.conflicts[k];
-            s_key[k] = b.mkeys[t];
-            s_task[k] = t;
-        } else {
-            s_key[k] = ~0ull;
-            s_task[k] = GBH_NONE;
-        }
-    }
+    if (threadIdx.x == 0) s_merged = 0;
     __syncthreads();
-    // bitonic sort by emission key
-    for (uint32_t size = 2; size <= P; size <<= 1) {
-        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            for (uint32_t k = threadIdx.x; k < P; k += blockDim.x) {
-                const uint32_t j = k ^ stride;
-                if (j > k) {
-                    const bool up = (k & size) == 0;
-                    const unsigned long long a = s_key[k], c = s_key[j];
-                    if ((a > c) == up) {
-                        s_key[k] = c;
-                        s_key[j] = a;
-                        const uint32_t tt = s_task[k];
-                        s_task[k] = s_task[j];
-                        s_task[j] = tt;
-                    }
-                }
-            }
-            __syncthreads();
+    uint32_t pending = C;
+    for (uint32_t round = 0; pending > 0 && round <= C; ++round) {
+        // the earliest pending key of every body of a pending task
+        for (uint32_t k = threadIdx.x; k < C; k += blockDim.x) {
+            const uint32_t e = list[k];
+            if (e & MERGE_DONE) continue;
+            const uint2 pr = b.mq->pairs[e];
+            const unsigned long long key = b.mkeys[e];
+            atomicMin(&first[pr.x], key);
+            atomicMin(&first[pr.y], key);
         }
+        if (threadIdx.x == 0) s_pending = 0;
+        __syncthreads();
+        // the tasks first on both bodies run (disjoint bodies); the rest wait
+        uint32_t merged = 0, left = 0;
+        for (uint32_t k = threadIdx.x; k < C; k += blockDim.x) {
+            const uint32_t e = list[k];
+            if (e & MERGE_DONE) continue;
+            const uint2 pr = b.mq->pairs[e];
+            const unsigned long long key = b.mkeys[e];
+            if (first[pr.x] == key && first[pr.y] == key) {
+                merged += apply_task(b, e, pr.x, pr.y) ? 1u : 0u;
+                list[k] = e | MERGE_DONE;
+            } else {
+                ++left;
+            }
+        }
+        if (merged) atomicAdd(&s_merged, merged);
+        if (left) atomicAdd(&s_pending, left);
+        __syncthreads();
+        pending = s_pending;
+        // forget this round's minima
+        for (uint32_t k = threadIdx.x; k < C; k += blockDim.x) {
+            const uint2 pr = b.mq->pairs[list[k] & ~MERGE_DONE];
+            first[pr.x] = ~0ull;
+            first[pr.y] = ~0ull;
+        }
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
-        uint32_t merged = 0;
-        for (uint32_t k = 0; k < C; ++k) {
-            const uint32_t t = s_task[k];
-            const uint2 pr = b.mq->pairs[t];
-            merged += apply_task(b, t, pr.x, pr.y) ? 1u : 0u;
-        }
-        b.st->merged += merged;
+        if (pending) set_error(b.st, GBH_DEVERR_MERGE_OVERFLOW);  // cannot happen: a round always runs a task
+        b.st->merged += s_merged;
     }
 }
 

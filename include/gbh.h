@@ -52,7 +52,7 @@ extern "C" {
 #define GBH_DEVERR_SORT_LOOKBACK 0x1u   /* onesweep look-back spin gave up (bounded wait) */
 #define GBH_DEVERR_FILL_SPIN 0x2u       /* bottom-up fill: frontier list overflow (cannot happen at its capacity N) */
 #define GBH_DEVERR_WALK_STACK 0x4u      /* a tree walk needed more stack than GBH_WALK_STACK */
-#define GBH_DEVERR_MERGE_OVERFLOW 0x8u  /* more conflicting merge tasks than one block can order */
+#define GBH_DEVERR_MERGE_OVERFLOW 0x8u  /* merge resolution did not finish (cannot happen: each round runs a task) */
 #define GBH_DEVERR_TREE_HEIGHT 0x10u    /* tree height above 64 (the reference fills only 64 levels) */
 #define GBH_DEVERR_MAC_FRONTIER 0x20u   /* learned walk frontier overflow */
 

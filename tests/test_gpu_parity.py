@@ -367,3 +367,37 @@ def test_derived_units_and_mid_run_update(gbh_lib, oracle_mod):
     pg, po = g.read_bodies()["pos_mass"], o.read_bodies()["pos_mass"]
     assert np.array_equal(pg[:, 3] == 0, po[:, 3] == 0)
     np.testing.assert_allclose(pg, po, rtol=1e-5, atol=1e-6)
+
+
+def test_merge_heavy_state_resolves_every_conflict(gbh_lib, oracle_mod):
+    # a cube so dense that most bodies overlap several others: thousands of
+    # merge tasks share bodies (chains of merges into one body); the
+    # resolution must equal the reference's one-thread schedule in emission
+    # order (the oracle) with no limit on the number of conflicts
+    from gravity_gb300 import ic
+
+    n = 60000
+    b = ic.uniform_merge(n, seed=12)
+    b["pos_mass"][:, :3] *= 0.03
+    bounds = np.array([-2, -2, -2, 2, 2, 2], np.float32)
+    g, o = make_pair(oracle_mod, BarnesHut, b, bounds)
+    p = abi.step_params(dt=5e-4, theta=0.7, softening=1e-8, mode=abi.MODE_MERGE, bounds=abi.BOUNDS_STATIC)
+    for x in (g, o):
+        x.stage_reset(p)
+        x.stage_prepare(p)
+        x.stage_sort()
+        x.stage_build()
+        x.stage_fill()
+        x.stage_walk(p)
+    tg, to = g.read_merge_tasks(), o.read_merge_tasks()
+    assert set(map(tuple, tg.tolist())) == set(map(tuple, to.tolist()))
+    g.stage_merge(p)
+    o.stage_merge(p)
+    sg, so = g.read_stats(), o.read_stats()
+    assert sg.error_word == 0
+    assert sg.merge_conflicts > 4096, sg.merge_conflicts
+    assert sg.merged == so.merged
+    bg, bo = g.read_bodies(abi.BODIES_OUT), o.read_bodies(abi.BODIES_OUT)
+    assert np.array_equal(bg["pos_mass"][:, 3] == 0, bo["pos_mass"][:, 3] == 0)
+    np.testing.assert_allclose(bg["pos_mass"], bo["pos_mass"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(bg["vel_density"], bo["vel_density"], rtol=1e-4, atol=1e-5)
