@@ -80,9 +80,10 @@ def workload(name: str, n: int | None, seed: int | None = None):
     if name == "clusters":
         # 256 Gaussian clusters, power-law masses, merges on, learned criterion
         n = n or 33554432
+        sd = 4 if seed is None else seed
         return dict(
-            name=f"cluster_mixture_n{n}",
-            bodies=lambda: ic.cluster_mixture(n, seed=4),
+            name=f"cluster_mixture_n{n}" + ("" if seed is None else f"_seed{sd}"),
+            bodies=lambda: ic.cluster_mixture(n, seed=sd),
             n=n,
             params=abi.step_params(dt=1e-3, theta=0.5, softening=0.005 ** 2, mode=abi.MODE_MERGE,
                                    bounds=abi.BOUNDS_DYNAMIC),
@@ -293,7 +294,7 @@ PLAIN_THETAS = [0.3, 0.5, 0.7]
 # DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture,
 # divided by its bodies; the walk's traffic grows in proportion to the bodies
-WALK_LEARNED_DRAM_BYTES_PER_BODY = 301.0
+WALK_LEARNED_DRAM_BYTES_PER_BODY = 297.6
 
 
 def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
@@ -342,15 +343,19 @@ def precision_arm(bh, p_plain, accuracy):
 
 
 def parse_sources(spec: str):
-    """'name[@seed]:share,...' -> [(name, seed or None, share)]"""
+    """'name[@seed][/bodies]:share,...' -> [(name, seed or None, bodies or None, share)]"""
     out = []
     for part in spec.split(","):
         name, share = part.split(":")
+        n = None
+        if "/" in name:
+            name, nb = name.split("/")
+            n = int(nb)
         seed = None
         if "@" in name:
             name, sd = name.split("@")
             seed = int(sd)
-        out.append((name, seed, float(share)))
+        out.append((name, seed, n, float(share)))
     return out
 
 
@@ -364,8 +369,8 @@ def train_out_of_sample(bh, args, local) -> dict:
 
     t0 = time.perf_counter()
     feats, labels, sources = [], [], []
-    for name, seed, share in parse_sources(args.train_sources):
-        wl = workload(name, None, seed) if seed is not None else workload(name, None)
+    for name, seed, nb, share in parse_sources(args.train_sources):
+        wl = workload(name, nb, seed) if name in ("mixture", "clusters") else workload(name, nb)
         b = wl["bodies"]()
         bounds = wl.get("bounds", ic.exact_bounds(b))
         p = abi.StepParams.from_buffer_copy(wl["params"])
@@ -447,6 +452,9 @@ def run_ours(args):
         mac_name = "plain+compensated"
     elif not (args.plain_only or wl.get("plain_only")):
         t0 = time.perf_counter()
+        if args.mac_band:
+            lo, hi = (float(x) for x in args.mac_band.split(","))
+            bh.mac_set_band(lo, hi)
         if args.mac_weights:
             bh.mac_set_weights(np.load(args.mac_weights))
             calib["weights"] = os.path.basename(args.mac_weights)
@@ -723,6 +731,8 @@ def main():
     ap.add_argument("--train-sources", default="galaxy:0.75,uniform_merge:0.25",
                     help="workloads whose snapshots give the training pairs, name[@seed]:share,... "
                          "(a seed only for the mixture)")
+    ap.add_argument("--mac-band", default=None,
+                    help="theta_accept,theta_open of the band the network decides (default 0.25,4)")
     ap.add_argument("--train-in-sample", action="store_true",
                     help="record the training pairs on the timed state itself (default: other workloads)")
     ap.add_argument("--save-mac-weights", default=None, help="save the trained MLP weights (.npy)")

@@ -42,6 +42,7 @@ MAC_HIDDEN = 32
 MAC_NUM_PARAMS = 32 * 12 + 32 + 32 * 32 + 32 + 32 + 1
 NONE_ID = 0xFFFFFFFF
 SORT_NOALLOC_MAX_PAIRS = 1 << 20  # GBH_SORT_NOALLOC_MAX_PAIRS
+SHARD_BYTES_PER_BODY = 36  # GBH_SHARD_BYTES_PER_BODY
 
 BODY_DTYPE = np.dtype([("pos_mass", "<f4", (4,)), ("vel_density", "<f4", (4,))])
 NODE_DTYPE = np.dtype(

@@ -110,12 +110,14 @@ class BarnesHut:
         self._chk(lib().gbh_step_shard_walk(self._h, C.byref(params), rank, world, r))
         return int(r[0]), int(r[1])
 
+    shard_bytes_per_body = abi.SHARD_BYTES_PER_BODY
+
     def shard_pack_tensor(self, lo: int, hi: int):
-        """The updated bodies of slots [lo, hi), slot order, as a uint8 tensor
-        on this context's GPU (the all-gather's send buffer)."""
+        """The updated bodies of slots [lo, hi), slot order, and their |a|, as
+        a uint8 tensor on this context's GPU (the all-gather's send buffer)."""
         import torch
 
-        t = torch.empty((hi - lo) * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device=f"cuda:{self.device}")
+        t = torch.empty((hi - lo) * abi.SHARD_BYTES_PER_BODY, dtype=torch.uint8, device=f"cuda:{self.device}")
         self._chk(lib().gbh_shard_pack(self._h, lo, hi - lo, C.c_void_p(t.data_ptr())))
         return t
 
@@ -125,7 +127,7 @@ class BarnesHut:
         import torch
 
         torch.cuda.current_stream(self.device).synchronize()
-        count = t.numel() // abi.BODY_DTYPE.itemsize
+        count = t.numel() // abi.SHARD_BYTES_PER_BODY
         self._chk(lib().gbh_shard_unpack(self._h, lo, count, C.c_void_p(t.data_ptr())))
 
     def read_merge_tasks_full(self):

@@ -7,7 +7,9 @@
 // reference walks every body independently of the others
 // (SH/compute/force/bh_force.comp:40-142), so a walk split by body equals the
 // whole walk body for body.  The updated bodies travel in sorted-slot order:
-// packed[i] = the output body of slot lo + i.
+// packed[i] = the output body of slot lo + i (32 bytes), followed by the
+// count magnitudes |a| of their walk (4 bytes each), which the learned
+// criterion reads in the next step (feature 8).
 #include "gbh_common.cuh"
 
 // The slots the walk updated: the plain walk its share [lo, hi); the group
@@ -49,20 +51,24 @@ void launch_shard_range(const StepBuffers& b, bool groups, cudaStream_t s) {
 }
 
 __global__ void k_shard_pack(StepBuffers b, uint32_t lo, uint32_t count, gbh_body* __restrict__ out) {
+    float* mag = reinterpret_cast<float*>(out + count);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t bi = b.idx_in[lo + i];
         st_body(out, i, ld_pos_mass(b.bodies_out, bi), ld_vel_density(b.bodies_out, bi));
+        mag[i] = b.accel_mag[bi];
     }
 }
 
 // the other ranks' bodies into the output buffer, and their positions into
 // the in-order copy the next compaction reads
 __global__ void k_shard_unpack(StepBuffers b, uint32_t lo, uint32_t count, const gbh_body* __restrict__ in) {
+    const float* mag = reinterpret_cast<const float*>(in + count);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t bi = b.idx_in[lo + i];
         const float4 pm = ld_pos_mass(in, i);
         st_body(b.bodies_out, bi, pm, ld_vel_density(in, i));
         b.sorted_pm[lo + i] = pm;
+        b.accel_mag[bi] = mag[i];
     }
 }
 

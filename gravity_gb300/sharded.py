@@ -10,9 +10,10 @@ the others (src/main/resources/shaders/compute/force/bh_force.comp:40-142), so
 the state after the step is bit for bit that of one unsharded step, on every
 rank.
 
-The exchange per step is the walk's output: 32 bytes per live body (position,
-mass, velocity, density; velocities travel too, because the shares move as the
-bodies' sorted order changes) plus the merge tasks.  The simulation object is
+The exchange per step is the walk's output: 36 bytes per live body (position,
+mass, velocity, density and the magnitude of the body's acceleration, which
+the learned criterion reads in the next step; velocities travel too, because
+the shares move as the bodies' sorted order changes) plus the merge tasks.  The simulation object is
 anything with the step_shard_* methods: gravity_gb300.BarnesHut (the GPU, with
 NCCL or gloo device all-gathers) or a CPU restatement with the same methods.
 """
@@ -41,7 +42,8 @@ class ShardedStep:
         ranges = [None] * self.world
         dist.all_gather_object(ranges, (lo, hi), group=g)
         # the updated bodies, padded to the largest share
-        width = max(h - l for l, h in ranges) * abi.BODY_DTYPE.itemsize
+        per = self.sim.shard_bytes_per_body
+        width = max(h - l for l, h in ranges) * per
         mine = self.sim.shard_pack_tensor(lo, hi)
         send = torch.zeros(max(width, 1), dtype=torch.uint8, device=mine.device)
         send[: mine.numel()] = mine
@@ -49,7 +51,7 @@ class ShardedStep:
         dist.all_gather(parts, send, group=g)
         for r, (l, h) in enumerate(ranges):
             if r != self.rank and h > l:
-                self.sim.shard_unpack_tensor(l, parts[r][: (h - l) * abi.BODY_DTYPE.itemsize])
+                self.sim.shard_unpack_tensor(l, parts[r][: (h - l) * per])
         # the merge tasks of every rank, in ordering-key order
         tasks = [None] * self.world
         dist.all_gather_object(tasks, self.sim.read_merge_tasks_full(), group=g)

@@ -268,7 +268,8 @@ int gbh_clear_error(gbh_ctx* ctx);
  *   1. gbh_step_shard_walk: reset, compaction, sort, build, fill and this
  *      rank's walk; range = the sorted slots [lo, hi) it updated (the ranks'
  *      ranges tile [0, n) in rank order);
- *   2. gbh_shard_pack: its updated bodies, slot order, into a DEVICE buffer;
+ *   2. gbh_shard_pack: its updated bodies, slot order, into a DEVICE buffer
+ *      (with their acceleration magnitudes: 36 bytes per body);
  *   3. the caller all-gathers the ranges and packed bodies (NCCL, or any
  *      transport), and gbh_shard_unpack installs every other rank's range;
  *   4. gbh_read_merge_tasks_full / gbh_write_merge_tasks: the caller gathers
@@ -279,6 +280,10 @@ int gbh_clear_error(gbh_ctx* ctx);
  * gbh_step on one rank.  FP32 form only (GBH_ERR_UNSUPPORTED otherwise). */
 int gbh_step_shard_walk(gbh_ctx* ctx, const gbh_step_params* params, uint32_t rank, uint32_t world,
                         uint32_t range[2]);
+/* the packed form of `count` updated bodies: count gbh_body records, then
+ * count floats |a| of their walk (the learned criterion reads them in the
+ * next step): GBH_SHARD_BYTES_PER_BODY bytes per body */
+#define GBH_SHARD_BYTES_PER_BODY 36u
 int gbh_shard_pack(gbh_ctx* ctx, uint32_t lo, uint32_t count, void* device_out);
 int gbh_shard_unpack(gbh_ctx* ctx, uint32_t lo, uint32_t count, const void* device_in);
 /* the last walk's merge tasks: pairs (body, other), ordering keys (sorted slot

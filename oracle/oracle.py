@@ -196,7 +196,10 @@ class OracleBarnesHut:
         _check(lib().orc_stage_walk_sample(self._h, C.byref(p), stride, C.byref(inter)), "walk_sample")
         return int(inter.value)
 
-    # the sharded step (same method names as gravity_gb300.BarnesHut)
+    # the sharded step (same method names as gravity_gb300.BarnesHut); the
+    # oracle walks with the plain rule only, so its records are the bodies
+    shard_bytes_per_body = abi.BODY_DTYPE.itemsize
+
     def step_shard_walk(self, p, rank: int, world: int) -> tuple[int, int]:
         r = (C.c_uint32 * 2)()
         _check(lib().orc_step_shard_walk(self._h, C.byref(p), rank, world, r), "step_shard_walk")

@@ -27,11 +27,13 @@ def _case(n=120000):
 
 def _sharded_step(sims, p):
     world = len(sims)
+    per = abi.SHARD_BYTES_PER_BODY
     ranges = [s.step_shard_walk(p, r, world) for r, s in enumerate(sims)]
     packed = [s.shard_pack_tensor(lo, hi) for s, (lo, hi) in zip(sims, ranges)]
     for r, s in enumerate(sims):
         for q, (lo, hi) in enumerate(ranges):
             if q != r and hi > lo:
+                assert packed[q].numel() == (hi - lo) * per
                 s.shard_unpack_tensor(lo, packed[q])
     tasks = [s.read_merge_tasks_full() for s in sims]
     pairs = np.concatenate([t[0] for t in tasks]).reshape(-1, 2)
