@@ -361,10 +361,12 @@ def parse_sources(spec: str):
 
 def train_out_of_sample(bh, args, local) -> dict:
     """The learned criterion's weights from training pairs recorded on
-    snapshots of other workloads (default: the two-galaxy encounter, 8,388,608
-    bodies, and the uniform cube with merges, 1,048,576 bodies), one step into
-    each run; the timed state is never seen in training.  Recording and
-    training are deterministic, so every run trains the same weights."""
+    snapshots of other states, one step into each run (default: the two-galaxy
+    encounter, 8,388,608 bodies; the uniform cube with merges, 1,048,576; a
+    Plummer + uniform mixture of 8,388,608 bodies drawn with seed 11; a
+    256-cluster mixture of 8,388,608 bodies drawn with seed 9); the timed
+    states (seeds 3 and 4) are never seen in training.  Recording and training
+    are deterministic, so every run trains the same weights."""
     from gravity_gb300 import BarnesHut
 
     t0 = time.perf_counter()
@@ -728,9 +730,10 @@ def main():
     ap.add_argument("--mac-tolerance", type=float, default=None, help="fixed tolerance instead of calibration")
     ap.add_argument("--mac-pairs", type=int, default=48_000_000,
                     help="training pairs (split 3:1 between the galaxy-pair and uniform-cube snapshots)")
-    ap.add_argument("--train-sources", default="galaxy:0.75,uniform_merge:0.25",
-                    help="workloads whose snapshots give the training pairs, name[@seed]:share,... "
-                         "(a seed only for the mixture)")
+    ap.add_argument("--train-sources",
+                    default="galaxy:0.4,uniform_merge:0.15,mixture@11/8388608:0.25,clusters@9/8388608:0.2",
+                    help="workloads whose snapshots give the training pairs, name[@seed][/bodies]:share,... "
+                         "(seeds for the mixture and the clusters; the defaults differ from the timed states')")
     ap.add_argument("--mac-band", default=None,
                     help="theta_accept,theta_open of the band the network decides (default 0.25,4)")
     ap.add_argument("--train-in-sample", action="store_true",
