@@ -275,7 +275,9 @@ __device__ __forceinline__ uint32_t atomic_add_acq_rel_cta(uint32_t* p, uint32_t
     return old;
 }
 
+#ifndef FILL_TILE
 #define FILL_TILE 512
+#endif
 
 // Tiled fill.  Block k owns the sorted slots [k T, k T + T) (T = FILL_TILE).
 // Phase 1: every thread initialises its leaf and keeps its values in shared
