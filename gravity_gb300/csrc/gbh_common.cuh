@@ -13,7 +13,9 @@
 #define GBH_NONE 0xFFFFFFFFu
 #define GBH_WARP 32
 #define GBH_WALK_STACK 192     // per-warp walk stack entries (tree height + 1 needed)
+#ifndef GBH_GROUP_MAX
 #define GBH_GROUP_MAX 96       // bodies per group of the group walk (one warp, three per lane)
+#endif
 #define GBH_MAX_TREE_HEIGHT_REF 64  // the reference fills 64 levels (GPU.java:41)
 
 // onesweep radix sort geometry (8-bit digits, 8 passes over the 63-bit key)

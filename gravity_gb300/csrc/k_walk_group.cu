@@ -373,6 +373,8 @@ __global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
             };
             if (nq >= GW_BPL)
                 slots(std::integral_constant<int, GW_BPL>{});
+            else if (GW_BPL > 3 && nq == 3)
+                slots(std::integral_constant<int, (GW_BPL > 3 ? 3 : 1)>{});
             else if (nq == 2)
                 slots(std::integral_constant<int, 2>{});
             else
