@@ -382,6 +382,8 @@ def train_out_of_sample(bh, args, local) -> dict:
         sim.upload_bodies(b)
         sim.init()
         sim.step(p)
+        if args.mac_band:  # pairs are recorded in the band the network will decide
+            sim.mac_set_band(*(float(x) for x in args.mac_band.split(",")))
         k = sim.mac_generate(p, max_pairs=int(args.mac_pairs * share), seed=1)
         f, lab = sim.mac_read_pairs(k)
         feats.append(f)
