@@ -35,7 +35,6 @@
 
 void launch_walk_group(const StepBuffers& b, const MacDeviceWeights& mw, bool learned, cudaStream_t s);
 void launch_walk_group_record(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s);
-void launch_find_groups(const StepBuffers& b, cudaStream_t s);
 int enqueue_reset(gbh_ctx* c);
 int enqueue_prepare(gbh_ctx* c);
 int enqueue_sort(gbh_ctx* c);
@@ -639,8 +638,7 @@ int gbh_mac_generate(gbh_ctx* c, const gbh_step_params* params, uint32_t max_pai
     //    candidates than the budget holds: a count pass first, then a hashed
     //    subset of (group, node) sized to about 95% of the budget, so the
     //    pairs come from every group rather than from the first ones to run.
-    launch_find_groups(ctx_buffers(c), c->stream);
-    const float thetas[2] = {0.25f, 0.6f};
+    const float thetas[2] = {0.25f, 0.6f};  // the groups come from the build above
     uint32_t start = 0;
     for (int r = 0; r < 2; ++r) {
         p.mac_mode = GBH_MAC_GROUP;

@@ -27,6 +27,29 @@ __device__ __forceinline__ int safe_lcp(const uint64_t* __restrict__ keys, int n
     return __clzll(a ^ c);
 }
 
+// Body groups of the group walks: the subtrees of at most GBH_GROUP_MAX
+// bodies whose parent holds more (every leaf lies in exactly one), as (first
+// sorted slot, body count).  A group is a contiguous range of sorted slots,
+// spatially compact because it is one tree node.  The build lists them: node
+// i knows its children's ranges, so an internal node with more than
+// GBH_GROUP_MAX bodies emits each child that holds at most that many; one
+// counter update per warp.
+__device__ __forceinline__ void emit_groups(const StepBuffers& b, uint32_t k, const uint2 (&mine)[2]) {
+    const uint32_t lane = lane_id();
+    uint32_t incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&b.st->num_groups, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    const uint32_t first = base + incl - k;
+    for (uint32_t q = 0; q < k; ++q) b.groups[first + q] = mine[q];
+}
+
 __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     const uint32_t n = b.st->n_new;
     const uint32_t N = b.N;
@@ -42,10 +65,15 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
             b.fill_ready[0] = 1;
             b.parent_int[0] = GBH_NONE;
             b.parent_leaf[0] = N;
+            b.groups[0] = make_uint2(0u, 1u);
+            b.st->num_groups = 1;
         }
         return;
     }
-    if (gid >= n - 1) return;
+    // every lane of a warp reaches the group list below
+    uint2 mine[2];
+    uint32_t k = 0;
+    if (gid < n - 1) {
     const int i = (int)gid, ni = (int)n;
     const int lcp_r = safe_lcp(keys, ni, i, i + 1);
     const int lcp_l = safe_lcp(keys, ni, i, i - 1);
@@ -76,6 +104,16 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     if (left < N) b.parent_leaf[left] = self; else b.parent_int[left - N] = self;
     if (right < N) b.parent_leaf[right] = self; else b.parent_int[right - N] = self;
     if (i == 0) b.parent_int[0] = GBH_NONE;
+    const uint32_t cnt = (uint32_t)(mx - mn + 1);
+    if (cnt > GBH_GROUP_MAX) {
+        const uint32_t cl = (uint32_t)(gamma - mn + 1), cr = (uint32_t)(mx - gamma);
+        if (cl <= GBH_GROUP_MAX) mine[k++] = make_uint2((uint32_t)mn, cl);
+        if (cr <= GBH_GROUP_MAX) mine[k++] = make_uint2((uint32_t)gamma + 1u, cr);
+    } else if (i == 0) {
+        mine[k++] = make_uint2(0u, cnt);  // the whole tree is one group
+    }
+    }
+    emit_groups(b, k, mine);
 }
 
 // The reference's Node topology words after buildBinaryRadixTree (childA/B,
@@ -105,6 +143,7 @@ void launch_build_nodes(const StepBuffers& b, cudaStream_t s) {
 
 void launch_build(const StepBuffers& b, cudaStream_t s) {
     const uint32_t nodes = b.N > 1 ? b.N - 1 : 1;
+    cudaMemsetAsync(&b.st->num_groups, 0, 4, s);
     k_build<<<(nodes + 255) / 256, 256, 0, s>>>(b);
 }
 

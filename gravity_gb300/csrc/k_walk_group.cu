@@ -2,7 +2,8 @@
 //
 // The reference decides per body (bh_force.comp:57-115).  Here a warp takes
 // one body group, a subtree of at most GBH_GROUP_MAX = 96 bodies (three per
-// lane; k_find_groups), and walks the tree once for all of its bodies:
+// lane; the build lists the groups, k_tree.cu), and walks the tree once for
+// all of its bodies:
 //   * candidates come off a per-warp stack 32 at a time, one per lane; each
 //     lane evaluates the acceptance criterion of the group against its node;
 //   * accepted nodes and leaves are appended to an interaction list, opened
@@ -81,59 +82,6 @@ struct GroupCfg {
     using Smem = GroupSmem<stack>;
     static constexpr size_t smem = MODE == GM_LEARNED ? sizeof(Smem) : offsetof(Smem, pend_cm);
 };
-
-// Body groups: the subtrees of at most GBH_GROUP_MAX bodies whose parent holds
-// more (every leaf lies in exactly one).  A group is a contiguous range of
-// sorted slots, spatially compact because it is one tree node.  Found from the
-// parent side: each internal node with more than GBH_GROUP_MAX bodies emits
-// its children that hold at most that many (the children's counts are read
-// only for the large nodes).
-__global__ void k_find_groups(StepBuffers b) {
-    const uint32_t n = b.st->n_new;
-    const uint32_t N = b.N;
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n == 1) {
-        if (t == 0) {
-            b.groups[0] = make_uint2(0u, 1u);
-            b.st->num_groups = 1;
-        }
-        return;
-    }
-    uint2 mine[2];
-    uint32_t k = 0;
-    if (t + 1 < n) {
-        const uint2 w = b.topo_kids[t];
-        const uint32_t cnt = b.topo_cnt[t];
-        if (cnt > GBH_GROUP_MAX) {
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const uint32_t ch = c == 0 ? w.x : w.y;
-                if (ch < N) {
-                    mine[k++] = make_uint2(ch, 1u);
-                } else {
-                    const uint32_t cc = b.topo_cnt[ch - N];
-                    if (cc <= GBH_GROUP_MAX) mine[k++] = make_uint2(b.node_lo[ch - N], cc);
-                }
-            }
-        } else if (t == 0) {
-            mine[k++] = make_uint2(0u, cnt);  // the whole tree is one group
-        }
-    }
-    // one counter update per warp
-    const uint32_t lane = lane_id();
-    uint32_t incl = k;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total) base = atomicAdd(&b.st->num_groups, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    const uint32_t first = base + incl - k;
-    for (uint32_t q = 0; q < k; ++q) b.groups[first + q] = mine[q];
-}
 
 // PREC: the precision form.  The lanes' bodies and the list entries are kept
 // relative to the group centre c_g: (x - c_g) + lo for a leaf (lo its FP32
@@ -643,14 +591,8 @@ void group_walk_setup() {
     set_smem<GM_RECORD, FORM_FP32>();
 }
 
-void launch_find_groups(const StepBuffers& b, cudaStream_t s) {
-    cudaMemsetAsync(&b.st->num_groups, 0, 4, s);
-    k_find_groups<<<(b.N + 255) / 256, 256, 0, s>>>(b);
-}
-
 template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
-    if (MODE != GM_RECORD) launch_find_groups(b, s);
     cudaMemsetAsync(&b.st->group_next, 0, 4, s);
     // persistent: the blocks that fit at once (no more than the groups need)
     const uint32_t need = (b.N + GW_WARPS * 32 - 1) / (GW_WARPS * 32) + 1;
@@ -676,7 +618,7 @@ void launch_walk_group(const StepBuffers& b, const MacDeviceWeights& mw, bool le
         launch_form<GM_THETA>(b, mw, s);
 }
 
-// the caller runs launch_find_groups once first: pairs name groups by index
+// pairs name groups by their index in the build's group list
 void launch_walk_group_record(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
     launch_mode<GM_RECORD, FORM_FP32>(b, mw, s);
 }
