@@ -35,26 +35,26 @@
 #include "gbh_ctx.h"
 #include "mac_mlp.cuh"
 
-#ifndef GW_THREADS
-#define GW_THREADS 256
-#endif
-#define GW_WARPS (GW_THREADS / 32)
 #define GW_STACK 768
 #define GW_LIST 64
 #define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
 #define GW_BPL (GBH_GROUP_MAX / 32)  // bodies per lane
-#ifdef GW_MINB_ALL
-#define GW_MINB(MODE, FORM) GW_MINB_ALL
-#else
-#define GW_MINB(MODE, FORM) (((MODE) == GM_THETA && (FORM) == FORM_FP32) ? 3 : 2)
-#endif
 
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 
+// Block shape per mode.  The learned walk runs 4-warp blocks, five per SM
+// (96 registers, 44 KB of shared memory each): 20 warps per SM, where 8-warp
+// blocks fit two (16 warps).  The others run 8-warp blocks.
+template <int MODE>
+struct GroupShape {
+    static constexpr int warps = MODE == GM_LEARNED ? 4 : 8;
+    static constexpr int threads = warps * 32;
+};
+
 // shared memory: the stacks and lists first, the network's tiles last (only
 // the learned walk allocates them).  The learned walk's stacks are shorter so
-// that three blocks fit on an SM.
-template <int STACK>
+// that more blocks fit on an SM.
+template <int STACK, int GW_WARPS>
 struct GroupSmem {
     uint32_t stack[GW_WARPS][STACK];
     float4 list_cm[GW_WARPS][GW_LIST];  // centre of mass, G x mass
@@ -79,7 +79,7 @@ struct GroupSmem {
 template <int MODE>
 struct GroupCfg {
     static constexpr int stack = MODE == GM_LEARNED ? GW_STACK_LEARNED : GW_STACK;
-    using Smem = GroupSmem<stack>;
+    using Smem = GroupSmem<stack, GroupShape<MODE>::warps>;
     static constexpr size_t smem = MODE == GM_LEARNED ? sizeof(Smem) : offsetof(Smem, pend_cm);
 };
 
@@ -92,8 +92,18 @@ struct GroupCfg {
 // form), FORM_MERGE (merge tasks from the leaf entries).
 enum GroupForm { FORM_FP32 = 0, FORM_PREC = 1, FORM_MERGE = 2 };
 
+// resident blocks per SM each instance is compiled for: the learned FP32 walk
+// five 4-warp blocks, its precision and merge forms four (their registers
+// need more than 96), the group-theta FP32 walk three 8-warp blocks, the rest
+// two
 template <int MODE, int FORM>
-__global__ __launch_bounds__(GW_THREADS, GW_MINB(MODE, FORM)) void k_walk_group(
+struct GroupMinBlocks {
+    static constexpr int value = MODE == GM_LEARNED ? (FORM == FORM_FP32 ? 5 : 4)
+                                 : (MODE == GM_THETA && FORM == FORM_FP32) ? 3 : 2;
+};
+
+template <int MODE, int FORM>
+__global__ __launch_bounds__(GroupShape<MODE>::threads, GroupMinBlocks<MODE, FORM>::value) void k_walk_group(
     StepBuffers b, MacDeviceWeights mw) {
     constexpr bool PREC = FORM == FORM_PREC;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -574,7 +584,8 @@ template <int MODE, int FORM>
 static void set_smem() {
     cudaFuncSetAttribute(k_walk_group<MODE, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)group_smem(MODE));
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_walk_group<MODE, FORM>, GW_THREADS, group_smem(MODE)) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_walk_group<MODE, FORM>, GroupShape<MODE>::threads,
+                                                      group_smem(MODE)) !=
             cudaSuccess ||
         nb < 1)
         nb = 1;
@@ -595,10 +606,11 @@ template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
     cudaMemsetAsync(&b.st->group_next, 0, 4, s);
     // persistent: the blocks that fit at once (no more than the groups need)
-    const uint32_t need = (b.N + GW_WARPS * 32 - 1) / (GW_WARPS * 32) + 1;
+    constexpr uint32_t threads = GroupShape<MODE>::threads;
+    const uint32_t need = (b.N + threads - 1) / threads + 1;
     uint32_t blocks = b.num_sms * (uint32_t)g_blocks_per_sm[MODE][FORM];
     if (blocks > need) blocks = need;
-    k_walk_group<MODE, FORM><<<blocks, GW_THREADS, group_smem(MODE), s>>>(b, mw);
+    k_walk_group<MODE, FORM><<<blocks, threads, group_smem(MODE), s>>>(b, mw);
 }
 
 template <int MODE>
