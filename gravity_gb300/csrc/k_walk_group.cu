@@ -39,6 +39,12 @@
 #define GW_LIST 64
 #define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
 #define GW_BPL (GBH_GROUP_MAX / 32)  // bodies per lane
+#ifndef GW_DECIDE_SP
+#define GW_DECIDE_SP 32u  // learned walk: decide the queue early below this stack depth...
+#endif
+#ifndef GW_DECIDE_NP
+#define GW_DECIDE_NP 20u  // ...when at least this many rows wait
+#endif
 
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
 
@@ -456,10 +462,11 @@ __global__ __launch_bounds__(GroupShape<MODE>::threads, GroupMinBlocks<MODE, FOR
     };
 
     while (sp > 0 || np > 0) {
-        // the network decides the queue before a pop when the stack cannot
-        // fill one and 20 or more rows wait: its opened nodes refill the
-        // stack, so pops run fuller (a decision does not depend on the batch)
-        if (MODE == GM_LEARNED && (sp == 0 || (sp < 32u && np >= 20u))) {
+        // the network decides the queue before a pop when the stack holds
+        // fewer than GW_DECIDE_SP nodes and GW_DECIDE_NP or more rows wait:
+        // its opened nodes refill the stack, so pops run fuller (a decision
+        // does not depend on the batch)
+        if (MODE == GM_LEARNED && (sp == 0 || (sp < GW_DECIDE_SP && np >= GW_DECIDE_NP))) {
             decide_queue(min(np, 32u));
             continue;
         }
