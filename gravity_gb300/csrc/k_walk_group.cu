@@ -40,7 +40,7 @@
 #define GW_QUEUE 64  // queued band candidates per warp: a full MLP batch + one pop
 #define GW_BPL (GBH_GROUP_MAX / 32)  // bodies per lane
 #ifndef GW_DECIDE_SP
-#define GW_DECIDE_SP 32u  // learned walk: decide the queue early below this stack depth...
+#define GW_DECIDE_SP 64u  // learned walk: decide the queue early below this stack depth...
 #endif
 #ifndef GW_DECIDE_NP
 #define GW_DECIDE_NP 20u  // ...when at least this many rows wait
