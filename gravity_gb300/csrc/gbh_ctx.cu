@@ -305,6 +305,8 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     char* base = (char*)c->arena;
     c->bodies[0] = (gbh_body*)(base + o_bodies0);
     c->bodies[1] = (gbh_body*)(base + o_bodies1);
+    c->body_phys[0] = c->bodies[0];
+    c->body_phys[1] = c->bodies[1];
     c->keys[0] = (uint64_t*)(base + o_keys0);
     c->keys[1] = (uint64_t*)(base + o_keys1);
     c->idx[0] = (uint32_t*)(base + o_idx0);
@@ -394,9 +396,9 @@ int gbh_destroy(gbh_ctx* c) {
         cudaStreamSynchronize(c->copy_stream2);
         cudaStreamDestroy(c->copy_stream2);
     }
-    for (cudaEvent_t e : {c->ev_in_ready, c->ev_in_free, c->ev_out_ready, c->ev_out_done})
+    for (cudaEvent_t e : {c->ev_in_ready, c->ev_out_ready, c->ev_out_done})
         if (e) cudaEventDestroy(e);
-    cudaFree(c->stage_in);
+    cudaFree(c->stage_alloc);  // stage_in and the state pointers may name any of the three buffers
     cudaFree(c->stage_out);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -446,16 +448,19 @@ int gbh_exchange_bodies(gbh_ctx* c, gbh_body* host_out, const gbh_body* host_in,
     return GBH_OK;
 }
 
-// Staging buffers, the second copy stream and the events of the streamed
-// steps, created on first use (two body buffers: 64 bytes per body).
+// The third body buffer, the result buffer of calls without a next input,
+// the second copy stream and the events of the streamed steps, created on
+// first use (two body buffers: 64 bytes per body).
 static int ensure_stream_buffers(gbh_ctx* c) {
-    if (c->stage_in) return GBH_OK;
+    if (c->stage_alloc) return GBH_OK;
     const size_t bytes = (size_t)c->N * sizeof(gbh_body);
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy_stream2, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&c->ev_in_ready, &c->ev_in_free, &c->ev_out_ready, &c->ev_out_done})
+    for (cudaEvent_t* e : {&c->ev_in_ready, &c->ev_out_ready, &c->ev_out_done})
         CUDA_TRY(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     CUDA_TRY(c, cudaMalloc(&c->stage_out, bytes));
-    CUDA_TRY(c, cudaMalloc(&c->stage_in, bytes));
+    CUDA_TRY(c, cudaMalloc(&c->stage_alloc, bytes));
+    c->stage_in = c->stage_alloc;
+    c->body_phys[2] = c->stage_alloc;
     return GBH_OK;
 }
 
@@ -466,35 +471,46 @@ int gbh_step_streamed(gbh_ctx* c, const gbh_step_params* p, const gbh_body* next
     int rc = ensure_stream_buffers(c);
     if (rc) return rc;
     const size_t bytes = (size_t)c->N * sizeof(gbh_body);
-    // the last call's result out of stage_out, once it is there
-    const bool give = c->stream_have_result && last_result;
-    if (give) {
+    // the last call's result, once it is there
+    if (c->stream_have_result && last_result) {
         CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream2, c->ev_out_ready, 0));
-        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->stage_out, bytes, cudaMemcpyDeviceToHost, c->copy_stream2));
+        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->result_buf, bytes, cudaMemcpyDeviceToHost, c->copy_stream2));
     }
     CUDA_TRY(c, cudaEventRecord(c->ev_out_done, c->copy_stream2));
-    // the next input into stage_in, once the last one has left it
+    // the next input into the third buffer; when that holds the last result,
+    // after the step that wrote it and the read-back above
     if (next_input) {
-        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_in_free, 0));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_out_ready, 0));
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_out_done, 0));
         CUDA_TRY(c, cudaMemcpyAsync(c->stage_in, next_input, bytes, cudaMemcpyHostToDevice, c->copy_stream));
         CUDA_TRY(c, cudaEventRecord(c->ev_in_ready, c->copy_stream));
     }
     // this call's step on the current state (one graph launch)
     if ((rc = gbh_step_n(c, p, 1))) return rc;
-    // its result into stage_out once the read-back above has finished with it
-    CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_out_done, 0));
-    CUDA_TRY(c, cudaMemcpyAsync(c->stage_out, c->bodies[c->bin], bytes, cudaMemcpyDeviceToDevice, c->stream));
-    CUDA_TRY(c, cudaEventRecord(c->ev_out_ready, c->stream));
-    c->stream_have_result = true;
+    gbh_body* const result = c->bodies[c->bin];
+    gbh_body* const consumed = c->bodies[1 - c->bin];
     if (next_input) {
-        // the next input becomes the current state
+        // rotate: the next input becomes the state, the consumed input the
+        // next step's output, and the result waits in the third slot for the
+        // next call's read-back (the step after this one does not touch it)
+        CUDA_TRY(c, cudaEventRecord(c->ev_out_ready, c->stream));
         CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_in_ready, 0));
-        CUDA_TRY(c, cudaMemcpyAsync(c->bodies[c->bin], c->stage_in, bytes, cudaMemcpyDeviceToDevice, c->stream));
-        CUDA_TRY(c, cudaEventRecord(c->ev_in_free, c->stream));
+        c->bodies[c->bin] = c->stage_in;
+        c->bodies[1 - c->bin] = consumed;
+        c->stage_in = result;
+        c->result_buf = result;
         c->pos64_valid = false;
         ++c->state_epoch;
         if ((rc = invalidate_sorted(c))) return rc;
+    } else {
+        // the result stays the state, which the step after next overwrites:
+        // the read-back takes a copy (once the last read-back has left it)
+        CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_out_done, 0));
+        CUDA_TRY(c, cudaMemcpyAsync(c->stage_out, result, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        CUDA_TRY(c, cudaEventRecord(c->ev_out_ready, c->stream));
+        c->result_buf = c->stage_out;
     }
+    c->stream_have_result = true;
     // the host buffers are free again; the step itself may still run
     CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream2));
@@ -507,7 +523,7 @@ int gbh_step_streamed_finish(gbh_ctx* c, gbh_body* last_result) {
     if (!c->stream_have_result) return fail(c, GBH_ERR_STATE, "no streamed step has run since the last finish");
     if (last_result) {
         CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream2, c->ev_out_ready, 0));
-        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->stage_out, (size_t)c->N * sizeof(gbh_body),
+        CUDA_TRY(c, cudaMemcpyAsync(last_result, c->result_buf, (size_t)c->N * sizeof(gbh_body),
                                     cudaMemcpyDeviceToHost, c->copy_stream2));
         CUDA_TRY(c, cudaStreamSynchronize(c->copy_stream2));
     }
@@ -653,10 +669,21 @@ int gbh_init(gbh_ctx* c) {
     return GBH_OK;
 }
 
+// which of the three body buffers a state pointer names (3: none)
+static int body_slot(const gbh_ctx* c, const gbh_body* p) {
+    for (int i = 0; i < 3; ++i)
+        if (c->body_phys[i] && c->body_phys[i] == p) return i;
+    return 3;
+}
+
+// A captured step names its buffers: the key holds the parities, the modes
+// and which body buffers are the step's input and output (streamed steps
+// rotate three).
 static int graph_key(const gbh_ctx* c) {
     return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2) |
            ((c->params_host.precision_mode == GBH_PRECISION_COMPENSATED) ? 16 : 0) |
-           ((int)c->params_host.merging_collision_or_neither << 5);
+           ((int)c->params_host.merging_collision_or_neither << 5) |
+           ((body_slot(c, c->bodies[c->bin]) * 4 + body_slot(c, c->bodies[1 - c->bin])) << 7);
 }
 
 int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1); }

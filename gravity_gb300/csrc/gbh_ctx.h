@@ -76,14 +76,21 @@ struct gbh_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_events[16] = {};
 
-    // gbh_step_streamed: the next input and the last result in device
-    // staging buffers (allocated on first use), the read-back on a second
-    // copy stream, and the events that order the copies with the steps
-    gbh_body* stage_in = nullptr;
+    // gbh_step_streamed: a third body buffer (allocated on first use) takes
+    // the next input; after the step the three rotate (the input becomes the
+    // state, the step's result waits for its read-back in the third buffer,
+    // the consumed input is the next output), so no body buffer is copied on
+    // the device.  A call without a next input keeps the result as the state
+    // and copies it to stage_out for the read-back.  The read-back runs on a
+    // second copy stream; events order the copies with the steps.
+    gbh_body* stage_in = nullptr;      // the free third buffer (rotates)
+    gbh_body* stage_alloc = nullptr;   // the third buffer's allocation
     gbh_body* stage_out = nullptr;
+    gbh_body* body_phys[3] = {};       // the three body buffers as allocated (graph keys name them)
+    gbh_body* result_buf = nullptr;    // where the last streamed step's result waits
     cudaStream_t copy_stream2 = nullptr;
-    cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_done = nullptr;
-    bool stream_have_result = false;  // stage_out holds the result of the last streamed step
+    cudaEvent_t ev_in_ready = nullptr, ev_out_ready = nullptr, ev_out_done = nullptr;
+    bool stream_have_result = false;  // result_buf holds the result of the last streamed step
 
     // sharded step (gbh_step_shard_walk ... gbh_step_shard_finish)
     uint32_t shard_rank = 0, shard_world = 1;  // the walk's share while a shard walk is enqueued

@@ -183,7 +183,8 @@ typedef struct gbh_stats {
 
 /* Device pointers of the live buffers, for headless consumers that replace the
  * reference's render shaders reading the same SSBOs (nodeglow.vert, regions.vert,
- * impostor.vert).  Valid until the next gbh_step (body/index buffers swap). */
+ * impostor.vert).  Valid until the next gbh_step (body/index buffers swap) or
+ * gbh_step_streamed (which rotates the body buffers through a third one). */
 typedef struct gbh_device_buffers {
     void* bodies_in;      /* gbh_body[initial_num_bodies] (current state) */
     void* bodies_out;

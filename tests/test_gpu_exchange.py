@@ -47,15 +47,18 @@ def test_streamed_steps_equal_upload_step_read(gbh_lib):
     # every call installs a new state and returns the previous call's result:
     # the results must be bit-identical to upload + step + read per state
     torch = pytest.importorskip("torch")
+    # (8 calls: the three body buffers rotate, so every pairing of input and
+    # output buffers and both parities come round)
     n = 70001
-    states = [ic.plummer(n, seed=10 + k) for k in range(4)]
+    calls = 8
+    states = [ic.plummer(n, seed=10 + k) for k in range(calls + 1)]
     bounds = ic.exact_bounds(states[0])
     p = abi.step_params(theta=0.5, softening=1e-4, bounds=abi.BOUNDS_DYNAMIC)
     ref = BarnesHut(n, bounds, abi.units(G=1.0))
     ref.upload_bodies(states[0])
     ref.init()
     want = []
-    for k in range(3):
+    for k in range(calls):
         ref.upload_bodies(states[k])
         ref.step(p)
         want.append(ref.read_bodies())
@@ -64,7 +67,7 @@ def test_streamed_steps_equal_upload_step_read(gbh_lib):
     sim.init()
     nxt, out = _pinned(torch, n), _pinned(torch, n)
     got = []
-    for k in range(3):
+    for k in range(calls):
         nxt[:] = states[k + 1]
         out.fill(0)
         sim.step_streamed(p, nxt, out)
@@ -72,10 +75,55 @@ def test_streamed_steps_equal_upload_step_read(gbh_lib):
             got.append(out.copy())
     sim.step_streamed_finish(out)
     got.append(out.copy())
-    for k in range(3):
+    for k in range(calls):
         assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), k
     # the last installed input is the current state
-    assert np.array_equal(sim.read_bodies().view(np.uint32), states[3].view(np.uint32))
+    assert np.array_equal(sim.read_bodies().view(np.uint32), states[calls].view(np.uint32))
+
+
+def test_streamed_steps_mixed_with_other_calls(gbh_lib):
+    # a pending result survives plain steps and uploads between streamed
+    # calls, with and without a next input
+    torch = pytest.importorskip("torch")
+    n = 60001
+    s = [ic.plummer(n, seed=30 + k) for k in range(5)]
+    bounds = ic.exact_bounds(s[0])
+    p = abi.step_params(theta=0.5, softening=1e-4, bounds=abi.BOUNDS_DYNAMIC)
+    ref = BarnesHut(n, bounds, abi.units(G=1.0))
+    ref.upload_bodies(s[0])
+    ref.init()
+
+    def run(state, steps):
+        ref.upload_bodies(state)
+        for _ in range(steps):
+            ref.step(p)
+        return ref.read_bodies()
+
+    r0 = run(s[0], 1)
+    r1 = run(s[1], 1)
+    r2 = run(r1, 2)
+    r3 = run(s[3], 1)
+    sim = BarnesHut(n, bounds, abi.units(G=1.0))
+    sim.upload_bodies(s[0])
+    sim.init()
+    pin, out = _pinned(torch, n), _pinned(torch, n)
+    pin[:] = s[1]
+    sim.step_streamed(p, pin, None)          # steps s0, installs s1
+    sim.step_streamed(p, None, out)          # returns r0, steps s1 (r1 stays the state)
+    assert np.array_equal(out.view(np.uint32), r0.view(np.uint32))
+    sim.step(p)                              # a plain step on r1
+    pin[:] = s[2]
+    sim.step_streamed(p, pin, out)           # returns r1, steps again, installs s2
+    assert np.array_equal(out.view(np.uint32), r1.view(np.uint32))
+    sim.upload_bodies(s[3])                  # replaces s2
+    pin[:] = s[4]
+    sim.step_streamed(p, pin, out)           # returns r2, steps s3, installs s4
+    assert np.array_equal(out.view(np.uint32), r2.view(np.uint32))
+    sim.step_streamed_finish(out)
+    assert np.array_equal(out.view(np.uint32), r3.view(np.uint32))
+    assert np.array_equal(sim.read_bodies().view(np.uint32), s[4].view(np.uint32))
+    sim.step(p)
+    assert np.array_equal(sim.read_bodies().view(np.uint32), run(s[4], 1).view(np.uint32))
 
 
 def test_streamed_steps_without_input_record_the_trajectory(gbh_lib):
