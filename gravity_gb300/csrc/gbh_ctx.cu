@@ -398,7 +398,10 @@ int gbh_destroy(gbh_ctx* c) {
     }
     for (cudaEvent_t e : {c->ev_in_ready, c->ev_out_ready, c->ev_out_done})
         if (e) cudaEventDestroy(e);
-    cudaFree(c->stage_alloc);  // stage_in and the state pointers may name any of the three buffers
+    // the role pointers (state, output, stage_in, spare) may name any of the
+    // four body buffers: free the allocations
+    cudaFree(c->stage_alloc[0]);
+    cudaFree(c->stage_alloc[1]);
     cudaFree(c->stage_out);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -448,19 +451,20 @@ int gbh_exchange_bodies(gbh_ctx* c, gbh_body* host_out, const gbh_body* host_in,
     return GBH_OK;
 }
 
-// The third body buffer, the result buffer of calls without a next input,
-// the second copy stream and the events of the streamed steps, created on
-// first use (two body buffers: 64 bytes per body).
+// The two rotating body buffers, the result buffer of calls without a next
+// input, the second copy stream and the events of the streamed steps,
+// created on first use (three body buffers: 96 bytes per body).
 static int ensure_stream_buffers(gbh_ctx* c) {
-    if (c->stage_alloc) return GBH_OK;
+    if (c->stage_alloc[0]) return GBH_OK;
     const size_t bytes = (size_t)c->N * sizeof(gbh_body);
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c->copy_stream2, cudaStreamNonBlocking));
     for (cudaEvent_t* e : {&c->ev_in_ready, &c->ev_out_ready, &c->ev_out_done})
         CUDA_TRY(c, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     CUDA_TRY(c, cudaMalloc(&c->stage_out, bytes));
-    CUDA_TRY(c, cudaMalloc(&c->stage_alloc, bytes));
-    c->stage_in = c->stage_alloc;
-    c->body_phys[2] = c->stage_alloc;
+    CUDA_TRY(c, cudaMalloc(&c->stage_alloc[0], bytes));
+    CUDA_TRY(c, cudaMalloc(&c->stage_alloc[1], bytes));
+    c->stage_in = c->body_phys[2] = c->stage_alloc[0];
+    c->spare = c->body_phys[3] = c->stage_alloc[1];
     return GBH_OK;
 }
 
@@ -477,11 +481,11 @@ int gbh_step_streamed(gbh_ctx* c, const gbh_step_params* p, const gbh_body* next
         CUDA_TRY(c, cudaMemcpyAsync(last_result, c->result_buf, bytes, cudaMemcpyDeviceToHost, c->copy_stream2));
     }
     CUDA_TRY(c, cudaEventRecord(c->ev_out_done, c->copy_stream2));
-    // the next input into the third buffer; when that holds the last result,
-    // after the step that wrote it and the read-back above
+    // the next input into stage_in: it held the result of the step before
+    // last, whose read-back the last call finished (each call waits for its
+    // copies), so only that step must have finished
     if (next_input) {
         CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_out_ready, 0));
-        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_out_done, 0));
         CUDA_TRY(c, cudaMemcpyAsync(c->stage_in, next_input, bytes, cudaMemcpyHostToDevice, c->copy_stream));
         CUDA_TRY(c, cudaEventRecord(c->ev_in_ready, c->copy_stream));
     }
@@ -491,13 +495,15 @@ int gbh_step_streamed(gbh_ctx* c, const gbh_step_params* p, const gbh_body* next
     gbh_body* const consumed = c->bodies[1 - c->bin];
     if (next_input) {
         // rotate: the next input becomes the state, the consumed input the
-        // next step's output, and the result waits in the third slot for the
-        // next call's read-back (the step after this one does not touch it)
+        // next step's output, the result waits in the spare slot for the next
+        // call's read-back, and the slot this call read back takes the next
+        // input
         CUDA_TRY(c, cudaEventRecord(c->ev_out_ready, c->stream));
         CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_in_ready, 0));
         c->bodies[c->bin] = c->stage_in;
         c->bodies[1 - c->bin] = consumed;
-        c->stage_in = result;
+        c->stage_in = c->spare;
+        c->spare = result;
         c->result_buf = result;
         c->pos64_valid = false;
         ++c->state_epoch;
@@ -669,21 +675,21 @@ int gbh_init(gbh_ctx* c) {
     return GBH_OK;
 }
 
-// which of the three body buffers a state pointer names (3: none)
+// which of the four body buffers a state pointer names (4: none)
 static int body_slot(const gbh_ctx* c, const gbh_body* p) {
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 4; ++i)
         if (c->body_phys[i] && c->body_phys[i] == p) return i;
-    return 3;
+    return 4;
 }
 
 // A captured step names its buffers: the key holds the parities, the modes
 // and which body buffers are the step's input and output (streamed steps
-// rotate three).
+// rotate four).
 static int graph_key(const gbh_ctx* c) {
     return (c->bin) | (c->iin << 1) | ((int)c->mac_mode << 2) |
            ((c->params_host.precision_mode == GBH_PRECISION_COMPENSATED) ? 16 : 0) |
            ((int)c->params_host.merging_collision_or_neither << 5) |
-           ((body_slot(c, c->bodies[c->bin]) * 4 + body_slot(c, c->bodies[1 - c->bin])) << 7);
+           ((body_slot(c, c->bodies[c->bin]) * 8 + body_slot(c, c->bodies[1 - c->bin])) << 7);
 }
 
 int gbh_step(gbh_ctx* c, const gbh_step_params* p) { return gbh_step_n(c, p, 1); }

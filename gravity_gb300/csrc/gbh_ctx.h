@@ -76,18 +76,22 @@ struct gbh_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_events[16] = {};
 
-    // gbh_step_streamed: a third body buffer (allocated on first use) takes
-    // the next input; after the step the three rotate (the input becomes the
-    // state, the step's result waits for its read-back in the third buffer,
-    // the consumed input is the next output), so no body buffer is copied on
-    // the device.  A call without a next input keeps the result as the state
-    // and copies it to stage_out for the read-back.  The read-back runs on a
-    // second copy stream; events order the copies with the steps.
-    gbh_body* stage_in = nullptr;      // the free third buffer (rotates)
-    gbh_body* stage_alloc = nullptr;   // the third buffer's allocation
+    // gbh_step_streamed: two more body buffers (allocated on first use), one
+    // taking the next input and one the result waiting for its read-back;
+    // after the step the four rotate (the input becomes the state, the
+    // consumed input the next output, the step's result waits for the next
+    // call's read-back, and the buffer read back by this call takes the next
+    // input), so no body buffer is copied on the device and the two copies
+    // never wait for each other.  A call without a next input keeps the
+    // result as the state and copies it to stage_out for the read-back.  The
+    // read-back runs on a second copy stream; events order the copies with
+    // the steps.
+    gbh_body* stage_in = nullptr;       // takes the next input (rotates)
+    gbh_body* spare = nullptr;          // the rotating result slot (rotates)
+    gbh_body* stage_alloc[2] = {};      // the two extra buffers' allocations
     gbh_body* stage_out = nullptr;
-    gbh_body* body_phys[3] = {};       // the three body buffers as allocated (graph keys name them)
-    gbh_body* result_buf = nullptr;    // where the last streamed step's result waits
+    gbh_body* body_phys[4] = {};        // the four body buffers as allocated (graph keys name them)
+    gbh_body* result_buf = nullptr;     // where the last streamed step's result waits
     cudaStream_t copy_stream2 = nullptr;
     cudaEvent_t ev_in_ready = nullptr, ev_out_ready = nullptr, ev_out_done = nullptr;
     bool stream_have_result = false;  // result_buf holds the result of the last streamed step

@@ -184,7 +184,7 @@ typedef struct gbh_stats {
 /* Device pointers of the live buffers, for headless consumers that replace the
  * reference's render shaders reading the same SSBOs (nodeglow.vert, regions.vert,
  * impostor.vert).  Valid until the next gbh_step (body/index buffers swap) or
- * gbh_step_streamed (which rotates the body buffers through a third one). */
+ * gbh_step_streamed (which rotates the body buffers through two more). */
 typedef struct gbh_device_buffers {
     void* bodies_in;      /* gbh_body[initial_num_bodies] (current state) */
     void* bodies_out;
@@ -237,7 +237,9 @@ int gbh_exchange_bodies(gbh_ctx* ctx, gbh_body* host_out, const gbh_body* host_i
  * first call: no result is copied.  Returns when both copies have finished
  * (the host buffers may be reused); the step itself may still be running.
  * gbh_step_streamed_finish copies the last call's result and waits for the
- * context.  The first call allocates two body-sized device buffers. */
+ * context.  The first call allocates three body-sized device buffers: the
+ * body buffers rotate through them, so no body buffer is copied on the device
+ * (device pointers from gbh_device_ptrs change with every call). */
 int gbh_step_streamed(gbh_ctx* ctx, const gbh_step_params* params, const gbh_body* next_input,
                       gbh_body* last_result);
 int gbh_step_streamed_finish(gbh_ctx* ctx, gbh_body* last_result);
