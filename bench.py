@@ -444,9 +444,10 @@ def train_out_of_sample(bh, args, local) -> dict:
 def kernels_per_step(mac_mode: int) -> int:
     """Kernels of this library launched by one step (the CUDA graph's kernel
     nodes): reset 1, prepare 3, sort 1 + 8 passes, build 1 (it also lists the
-    group walks' body groups), fill 2, walk 1, merge resolution 4 (they exit
-    at once without merge tasks), swap 0 (a pointer swap)."""
-    return 1 + 3 + 9 + 1 + 2 + 1 + 4
+    group walks' body groups), fill 2, walk 1 (the group and learned walks 2:
+    the groups' start lists, then the walk), merge resolution 4 (they exit at
+    once without merge tasks), swap 0 (a pointer swap)."""
+    return 1 + 3 + 9 + 1 + 2 + (1 if mac_mode == abi.MAC_PLAIN else 2) + 4
 
 
 def run_ours(args):

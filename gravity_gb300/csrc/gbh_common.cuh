@@ -16,6 +16,9 @@
 #ifndef GBH_GROUP_MAX
 #define GBH_GROUP_MAX 96       // bodies per group of the group walk (one warp, three per lane)
 #endif
+// words per group of the group walks' start lists: a count and up to 63 nodes
+// (deeper groups start from the root)
+#define GBH_PATH_WORDS 64
 #define GBH_MAX_TREE_HEIGHT_REF 64  // the reference fills 64 levels (GPU.java:41)
 
 // onesweep radix sort geometry (8-bit digits, 8 passes over the 63-bit key)
@@ -116,6 +119,12 @@ struct StepBuffers {
     uint32_t* parent_int;  // parentId per internal node
     uint32_t* parent_leaf; // parentId per leaf
     uint2* groups;        // (first slot, body count) of the group walk's body groups
+    uint32_t* group_node; // per group: the node whose subtree it is (global id)
+    // per group (below group_path_cap): where its walk starts, word 0 the
+    // count (0: from the root), then the group's own node and the siblings of
+    // its ancestors (k_group_paths)
+    uint32_t* group_path;
+    uint32_t group_path_cap;
     uint2* fill_frontier; // (node, bodies) handed from the tiled fill to the top-tree fill
     uint32_t fill_frontier_cap;
     // precision form (GBH_PRECISION_COMPENSATED); null until first used
@@ -324,6 +333,7 @@ void launch_sort_hist(const uint64_t* keys, uint32_t n, uint32_t* hist, DevState
 void launch_generate_bodies(gbh_body* bodies, uint32_t count, uint32_t offset, const gbh_ic_params& p, uint64_t seed,
                             cudaStream_t s);
 void launch_build(const StepBuffers& b, cudaStream_t s);
+void launch_group_paths(const StepBuffers& b, cudaStream_t s);
 void launch_fill(const StepBuffers& b, cudaStream_t s);
 void launch_build_nodes(const StepBuffers& b, cudaStream_t s);
 void launch_walk_plain(const StepBuffers& b, cudaStream_t s);

@@ -82,6 +82,9 @@ StepBuffers ctx_buffers(const gbh_ctx* c) {
     b.parent_int = c->parent_int;
     b.parent_leaf = c->parent_leaf;
     b.groups = c->groups;
+    b.group_node = c->group_node;
+    b.group_path = c->group_path;
+    b.group_path_cap = c->group_path_cap;
     // the fill's frontier lives in the sort's spare key buffer (free once the
     // sorted keys are back in keys_in, until the next step's encode)
     b.fill_frontier = reinterpret_cast<uint2*>(c->keys[1 - c->iin]);
@@ -289,7 +292,11 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     size_t o_mq = A.add(8 + (size_t)n * 8), o_mkeys = A.add((size_t)n * 8), o_mslots = A.add((size_t)n * 4);
     size_t o_locks = A.add((size_t)n * 4), o_conf = A.add((size_t)n * 4);
     size_t o_accel = A.add((size_t)n * 16), o_amag = A.add((size_t)n * 4);
-    size_t o_nlo = A.add((size_t)ni * 4), o_groups = A.add((size_t)n * 8);
+    size_t o_nlo = A.add((size_t)ni * 4), o_groups = A.add((size_t)n * 8), o_gnode = A.add((size_t)n * 4);
+    // start lists for one group per 16 bodies (groups hold up to 96, about 60
+    // on average; the groups past the capacity start from the root)
+    c->group_path_cap = n / 16 + 64;
+    size_t o_gpath = A.add((size_t)c->group_path_cap * GBH_PATH_WORDS * 4);
     size_t o_tkids = A.add((size_t)ni * 8), o_tcnt = A.add((size_t)ni * 4), o_tready = A.add((size_t)ni * 4);
     size_t o_pint = A.add((size_t)ni * 4), o_pleaf = A.add((size_t)n * 4);
     size_t o_tdead = A.add((size_t)c->prep_tiles_cap * 4), o_taabb = A.add((size_t)c->prep_tiles_cap * 24);
@@ -335,6 +342,8 @@ int gbh_create(gbh_ctx** out, uint32_t n, const float bounds[6], const gbh_units
     c->parent_leaf = (uint32_t*)(base + o_pleaf);
     c->node_lo = (uint32_t*)(base + o_nlo);
     c->groups = (uint2*)(base + o_groups);
+    c->group_node = (uint32_t*)(base + o_gnode);
+    c->group_path = (uint32_t*)(base + o_gpath);
     c->tile_dead = (uint32_t*)(base + o_tdead);
     c->tile_aabb = (float*)(base + o_taabb);
     c->hist = (uint32_t*)(base + o_hist);

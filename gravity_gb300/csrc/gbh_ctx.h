@@ -50,6 +50,9 @@ struct gbh_ctx {
     uint32_t* parent_int = nullptr;
     uint32_t* parent_leaf = nullptr;
     uint2* groups = nullptr;
+    uint32_t* group_node = nullptr;
+    uint32_t* group_path = nullptr;
+    uint32_t group_path_cap = 0;
     uint32_t* tile_dead = nullptr;
     float* tile_aabb = nullptr;
     uint32_t* hist = nullptr;

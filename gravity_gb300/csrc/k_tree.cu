@@ -34,7 +34,8 @@ __device__ __forceinline__ int safe_lcp(const uint64_t* __restrict__ keys, int n
 // i knows its children's ranges, so an internal node with more than
 // GBH_GROUP_MAX bodies emits each child that holds at most that many; one
 // counter update per warp.
-__device__ __forceinline__ void emit_groups(const StepBuffers& b, uint32_t k, const uint2 (&mine)[2]) {
+__device__ __forceinline__ void emit_groups(const StepBuffers& b, uint32_t k, const uint2 (&mine)[2],
+                                            const uint32_t (&node)[2]) {
     const uint32_t lane = lane_id();
     uint32_t incl = k;
 #pragma unroll
@@ -47,7 +48,10 @@ __device__ __forceinline__ void emit_groups(const StepBuffers& b, uint32_t k, co
     if (lane == 31 && total) base = atomicAdd(&b.st->num_groups, total);
     base = __shfl_sync(0xffffffffu, base, 31);
     const uint32_t first = base + incl - k;
-    for (uint32_t q = 0; q < k; ++q) b.groups[first + q] = mine[q];
+    for (uint32_t q = 0; q < k; ++q) {
+        b.groups[first + q] = mine[q];
+        b.group_node[first + q] = node[q];
+    }
 }
 
 __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
@@ -66,12 +70,14 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
             b.parent_int[0] = GBH_NONE;
             b.parent_leaf[0] = N;
             b.groups[0] = make_uint2(0u, 1u);
+            b.group_node[0] = N;
             b.st->num_groups = 1;
         }
         return;
     }
     // every lane of a warp reaches the group list below
     uint2 mine[2];
+    uint32_t mine_node[2] = {0u, 0u};
     uint32_t k = 0;
     if (gid < n - 1) {
     const int i = (int)gid, ni = (int)n;
@@ -107,13 +113,20 @@ __global__ __launch_bounds__(256) void k_build(StepBuffers b) {
     const uint32_t cnt = (uint32_t)(mx - mn + 1);
     if (cnt > GBH_GROUP_MAX) {
         const uint32_t cl = (uint32_t)(gamma - mn + 1), cr = (uint32_t)(mx - gamma);
-        if (cl <= GBH_GROUP_MAX) mine[k++] = make_uint2((uint32_t)mn, cl);
-        if (cr <= GBH_GROUP_MAX) mine[k++] = make_uint2((uint32_t)gamma + 1u, cr);
+        if (cl <= GBH_GROUP_MAX) {
+            mine_node[k] = left;
+            mine[k++] = make_uint2((uint32_t)mn, cl);
+        }
+        if (cr <= GBH_GROUP_MAX) {
+            mine_node[k] = right;
+            mine[k++] = make_uint2((uint32_t)gamma + 1u, cr);
+        }
     } else if (i == 0) {
+        mine_node[k] = N;
         mine[k++] = make_uint2(0u, cnt);  // the whole tree is one group
     }
     }
-    emit_groups(b, k, mine);
+    emit_groups(b, k, mine, mine_node);
 }
 
 // The reference's Node topology words after buildBinaryRadixTree (childA/B,
@@ -139,6 +152,43 @@ __global__ void k_build_nodes(StepBuffers b) {
 
 void launch_build_nodes(const StepBuffers& b, cudaStream_t s) {
     k_build_nodes<<<(b.N + 255) / 256, 256, 0, s>>>(b);
+}
+
+// Where each group's walk starts: the group's own subtree and the sibling of
+// every ancestor of it, which together hold every body once.  A walk from the
+// root opens each ancestor of the group anyway (its box holds the group's
+// bodies), one level per round of candidates; starting from this list gives
+// the same accepted and listed nodes without those rounds.  One thread per
+// group climbs the parent links; a group deeper than GBH_PATH_WORDS - 2
+// levels, or past the list's capacity, starts from the root (count 0).
+__global__ __launch_bounds__(256) void k_group_paths(StepBuffers b) {
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ng = min(b.st->num_groups, b.group_path_cap);
+    if (gi >= ng) return;
+    const uint32_t N = b.N, root = N;
+    uint32_t* out = b.group_path + (size_t)gi * GBH_PATH_WORDS;
+    uint32_t node = b.group_node[gi];
+    uint32_t len = 0;
+    out[1 + len++] = node;
+    while (node != root && len < GBH_PATH_WORDS - 1) {
+        const uint32_t p = node < N ? b.parent_leaf[node] : b.parent_int[node - N];
+        if (p < N || p - N >= N) {  // not an internal node: leave the group to the root start
+            len = 0;
+            break;
+        }
+        const uint2 kids = b.topo_kids[p - N];
+        out[1 + len++] = kids.x == node ? kids.y : kids.x;
+        node = p;
+    }
+    if (node != root) len = 0;
+    out[0] = len;
+}
+
+void launch_group_paths(const StepBuffers& b, cudaStream_t s) {
+    // the groups of the step are counted on the device: enough threads for
+    // the list's capacity, the surplus returns at once
+    const uint32_t threads = min(b.N, b.group_path_cap);
+    k_group_paths<<<(threads + 255) / 256, 256, 0, s>>>(b);
 }
 
 void launch_build(const StepBuffers& b, cudaStream_t s) {

@@ -237,9 +237,20 @@ __global__ __launch_bounds__(GroupShape<MODE>::threads, GroupMinBlocks<MODE, FOR
         cx_[q] = cy_[q] = cz_[q] = cp_[q] = 0.f;
     }
     uint32_t inter = 0, evals = 0, opened = 0;
-    uint32_t sp = n > 1 ? 1u : 0u, ln = 0, np = 0;
+    uint32_t sp = 0, ln = 0, np = 0;
     bool saturated = false;
-    if (lane == 0) stk[0] = N;  // root
+    if (n > 1) {
+        // the group's start list (its own subtree and the siblings of its
+        // ancestors, k_group_paths) when it has one, else the root
+        const uint32_t* path = b.group_path + (size_t)gi * GBH_PATH_WORDS;
+        sp = gi < b.group_path_cap ? path[0] : 0u;
+        if (sp == 0) {
+            if (lane == 0) stk[0] = N;
+            sp = 1;
+        } else {
+            for (uint32_t k = lane; k < sp; k += 32) stk[k] = path[1 + k];
+        }
+    }
     __syncwarp();
 
     // forces of list entries [0, cnt) on every lane's own body.  With a
@@ -611,6 +622,7 @@ void group_walk_setup() {
 
 template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
+    launch_group_paths(b, s);
     cudaMemsetAsync(&b.st->group_next, 0, 4, s);
     // persistent: the blocks that fit at once (no more than the groups need)
     constexpr uint32_t threads = GroupShape<MODE>::threads;
