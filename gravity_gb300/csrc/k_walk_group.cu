@@ -43,7 +43,7 @@
 #define GW_DECIDE_SP 64u  // learned walk: decide the queue early below this stack depth...
 #endif
 #ifndef GW_DECIDE_NP
-#define GW_DECIDE_NP 20u  // ...when at least this many rows wait
+#define GW_DECIDE_NP 16u  // ...when at least this many rows wait
 #endif
 
 enum GroupMode { GM_THETA = 0, GM_LEARNED = 1, GM_RECORD = 2 };
@@ -240,15 +240,20 @@ __global__ __launch_bounds__(GroupShape<MODE>::threads, GroupMinBlocks<MODE, FOR
     uint32_t sp = 0, ln = 0, np = 0;
     bool saturated = false;
     if (n > 1) {
-        // the group's start list (its own subtree and the siblings of its
-        // ancestors, k_group_paths) when it has one, else the root
+        // the group's start list when it has one (k_group_paths: its own
+        // subtree, then the siblings of its ancestors), else the root.  The
+        // group's own subtree enters as its leaves, sorted slots [first,
+        // first + count): a walk opens every internal node of it (their boxes
+        // hold group bodies) and lists every leaf.
         const uint32_t* path = b.group_path + (size_t)gi * GBH_PATH_WORDS;
-        sp = gi < b.group_path_cap ? path[0] : 0u;
-        if (sp == 0) {
+        const uint32_t len = gi < b.group_path_cap ? path[0] : 0u;
+        if (len == 0) {
             if (lane == 0) stk[0] = N;
             sp = 1;
         } else {
-            for (uint32_t k = lane; k < sp; k += 32) stk[k] = path[1 + k];
+            for (uint32_t k = lane; k < len - 1; k += 32) stk[k] = path[2 + k];
+            for (uint32_t k = lane; k < grp.y; k += 32) stk[len - 1 + k] = grp.x + k;
+            sp = len - 1 + grp.y;
         }
     }
     __syncwarp();
