@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import subprocess
@@ -294,7 +295,7 @@ PLAIN_THETAS = [0.3, 0.5, 0.7]
 # DRAM bytes per body of one learned-walk launch: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of k_walk_group<1> on the 4,194,304-body mixture,
 # divided by its bodies; the walk's traffic grows in proportion to the bodies
-WALK_LEARNED_DRAM_BYTES_PER_BODY = 301.3
+WALK_LEARNED_DRAM_BYTES_PER_BODY = 284.8
 
 
 def timed_steps(bh, p, steps, warmup, stream, dist, local, clocks=None):
@@ -635,6 +636,17 @@ def run_ours(args):
     bh.step_streamed_finish(None)
 
     def e2e_run(form):
+        # the harness's own garbage collector is paused for the timed calls
+        # (a collection of this process's heap is a host stall of tens of ms
+        # that a host in another language would not have)
+        gc.collect()
+        gc.disable()
+        try:
+            return _e2e_run(form)
+        finally:
+            gc.enable()
+
+    def _e2e_run(form):
         barrier(dist, local)
         t0 = time.perf_counter()
         if form == "streamed":
