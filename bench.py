@@ -445,10 +445,10 @@ def train_out_of_sample(bh, args, local) -> dict:
 def kernels_per_step(mac_mode: int) -> int:
     """Kernels of this library launched by one step (the CUDA graph's kernel
     nodes): reset 1, prepare 3, sort 1 + 8 passes, build 1 (it also lists the
-    group walks' body groups), fill 2, walk 1 (the group and learned walks 2:
-    the groups' start lists, then the walk), merge resolution 4 (they exit at
+    group walks' body groups; with the group and learned walks 2: then the
+    groups' start lists), fill 2, walk 1, merge resolution 4 (they exit at
     once without merge tasks), swap 0 (a pointer swap)."""
-    return 1 + 3 + 9 + 1 + 2 + (1 if mac_mode == abi.MAC_PLAIN else 2) + 4
+    return 1 + 3 + 9 + (1 if mac_mode == abi.MAC_PLAIN else 2) + 2 + 1 + 4
 
 
 def run_ours(args):
@@ -646,13 +646,18 @@ def run_ours(args):
         finally:
             gc.enable()
 
+    call_ms = []
+
     def _e2e_run(form):
         barrier(dist, local)
         t0 = time.perf_counter()
         if form == "streamed":
+            call_ms.append([])
             bh.upload_bodies(pin_in, chunk=n)
             for k in range(e2e_steps):
+                tc = time.perf_counter()
                 bh.step_streamed(p_head, pin_in if k + 1 < e2e_steps else None, pin_out if k else None)
+                call_ms[-1].append(round((time.perf_counter() - tc) * 1e3, 2))
             bh.step_streamed_finish(pin_out)
         elif form == "exchange":
             bh.upload_bodies(pin_in, chunk=n)
@@ -672,11 +677,16 @@ def run_ours(args):
     e2e_exchange_s = e2e_run("exchange")
     # the headline form five times (a host stall in one run of 20 steps
     # moves it by up to a tenth): the median, with all five kept
+    e2e_clocks = ClockSampler(local)
+    e2e_clocks.start()
     e2e_runs = [e2e_run("streamed") for _ in range(5)]
+    e2e_clk = e2e_clocks.stop()
     e2e_s = sorted(e2e_runs)[2]
     e2e = {
         "value": world * e2e_steps / e2e_s,
         "runs": [world * e2e_steps / t for t in e2e_runs],
+        "call_ms": call_ms,  # host time of each streamed call, per run
+        "clocks": e2e_clk,
         "unit": "steps/s",
         "h2d_bytes_per_step": n * abi.BODY_DTYPE.itemsize + C.sizeof(abi.StepParams),
         "d2h_bytes_per_step": n * abi.BODY_DTYPE.itemsize,

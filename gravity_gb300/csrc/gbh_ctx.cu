@@ -138,6 +138,10 @@ int enqueue_sort(gbh_ctx* c) {
 
 int enqueue_build(gbh_ctx* c) {
     launch_build(ctx_buffers(c), c->stream);
+    // the group walks' start lists belong to the tree: built with it when a
+    // group walk is selected (otherwise the group walk builds them itself)
+    c->paths_current = c->mac_mode != GBH_MAC_PLAIN;
+    if (c->paths_current) launch_group_paths(ctx_buffers(c), c->stream);
     return check_launch(c, "build");
 }
 

@@ -53,6 +53,7 @@ struct gbh_ctx {
     uint32_t* group_node = nullptr;
     uint32_t* group_path = nullptr;
     uint32_t group_path_cap = 0;
+    bool paths_current = false;  // the start lists describe the current tree (enqueue_build)
     uint32_t* tile_dead = nullptr;
     float* tile_aabb = nullptr;
     uint32_t* hist = nullptr;

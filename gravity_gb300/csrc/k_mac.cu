@@ -528,6 +528,10 @@ static MacDeviceWeights mac_weights(const gbh_ctx* c) {
 int enqueue_walk_learned(gbh_ctx* c) {
     const bool learned = c->mac_mode == GBH_MAC_LEARNED;
     if (learned && (!c->mac || !c->mac_ready)) return mac_fail(c, GBH_ERR_STATE, "learned MAC without weights");
+    if (!c->paths_current) {  // the tree was built for the plain walk
+        launch_group_paths(ctx_buffers(c), c->stream);
+        c->paths_current = true;
+    }
     launch_walk_group(ctx_buffers(c), mac_weights(c), learned, c->stream);
     return GBH_OK;
 }

@@ -627,7 +627,9 @@ void group_walk_setup() {
 
 template <int MODE, int FORM>
 static void launch_mode(const StepBuffers& b, const MacDeviceWeights& mw, cudaStream_t s) {
-    launch_group_paths(b, s);
+    // the step's walks find the start lists built with the tree
+    // (enqueue_build); the recording walk builds its own
+    if (MODE == GM_RECORD) launch_group_paths(b, s);
     cudaMemsetAsync(&b.st->group_next, 0, 4, s);
     // persistent: the blocks that fit at once (no more than the groups need)
     constexpr uint32_t threads = GroupShape<MODE>::threads;
