@@ -398,14 +398,18 @@ def parse_sources(spec: str):
     return out
 
 
-def train_out_of_sample(bh, args, local) -> dict:
+def train_out_of_sample(bh, args, local, held: list) -> dict:
     """The learned criterion's weights from training pairs recorded on
     snapshots of other states, one step into each run (default: the two-galaxy
     encounter, 8,388,608 bodies; the uniform cube with merges, 1,048,576; a
     Plummer + uniform mixture of 8,388,608 bodies drawn with seed 11; a
     256-cluster mixture of 8,388,608 bodies drawn with seed 9); the timed
     states (seeds 3 and 4) are never seen in training.  Recording and training
-    are deterministic, so every run trains the same weights."""
+    are deterministic, so every run trains the same weights.  The snapshot
+    contexts go to `held` and stay open until the run ends: on the GB300 machine,
+    destroying a context of several GB (cudaFree of its arena) left later
+    CUDA calls of the process with host stalls of 20 to 90 ms about twice a
+    second, which the streamed end-to-end calls then measured."""
     from gravity_gb300 import BarnesHut
 
     t0 = time.perf_counter()
@@ -417,6 +421,9 @@ def train_out_of_sample(bh, args, local) -> dict:
         p = abi.StepParams.from_buffer_copy(wl["params"])
         p.merging_collision_or_neither = abi.MODE_NEITHER  # the field only
         p.precision_mode = abi.PRECISION_FP32
+        import torch
+
+        free_before = torch.cuda.mem_get_info(local)[0]
         sim = BarnesHut(wl["n"], bounds, abi.units(G=1.0), device=local)
         sim.upload_bodies(b)
         sim.init()
@@ -428,7 +435,7 @@ def train_out_of_sample(bh, args, local) -> dict:
         feats.append(f)
         labels.append(lab)
         sources.append({"workload": wl["name"], "pairs": int(k)})
-        sim.close()
+        held.append((sim, free_before - torch.cuda.mem_get_info(local)[0]))
     F = np.concatenate(feats)
     L = np.concatenate(labels)
     t1 = time.perf_counter()
@@ -458,6 +465,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from gravity_gb300 import BarnesHut, accuracy
 
+    held = []  # contexts kept open until the run ends (train_out_of_sample)
     wl = workload(args.workload, args.n)
     bodies = wl["bodies"]()
     bounds = wl.get("bounds", ic.exact_bounds(bodies))
@@ -512,7 +520,7 @@ def run_ours(args):
                                  "loss_last": float(losses[-1]), "seconds": time.perf_counter() - t0}
             calib["weights_source"] = "in-sample: trained on the timed state"
         else:
-            calib["training"] = train_out_of_sample(bh, args, local)
+            calib["training"] = train_out_of_sample(bh, args, local, held)
             calib["weights_source"] = "out-of-sample: " + args.train_sources
         ref_sample = accuracy.DirectSumSample(bh, p_plain, count=4096, seed=2)
         calib["judge"] = ref_sample.judge
@@ -565,7 +573,9 @@ def run_ours(args):
     st_prof = bh.read_stats()
 
     # ---- comparison arms on the same context, same timing rules
-    footprint = free0 - torch.cuda.mem_get_info(local)[0]
+    # the context's own footprint (the training snapshots' contexts, still
+    # open, are not part of it)
+    footprint = free0 - torch.cuda.mem_get_info(local)[0] - sum(nbytes for _, nbytes in held)
     compare = {}
     if precision and not args.no_compare:
         ms_p, st_p, _ = timed_steps(bh, p_plain, args.steps, args.warmup, stream, dist, local)
@@ -704,6 +714,8 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, bodies, bounds, units, budget_s=args.cpu_budget)
+    for sim, _ in held:  # the training snapshots' contexts (see train_out_of_sample)
+        sim.close()
     if rank != 0:
         return 0
     line = {
