@@ -739,6 +739,9 @@ int gbh_step_n(gbh_ctx* c, const gbh_step_params* p, uint32_t count) {
             it = c->graphs.emplace(key, ex).first;
         }
         CUDA_TRY(c, cudaGraphLaunch(it->second, c->stream));
+        // the graph's build stage ran for this mode (the key holds it): the
+        // start lists are current exactly when a group walk is selected
+        c->paths_current = c->mac_mode != GBH_MAC_PLAIN;
         // the step flips both the body buffers and the (morton, index) buffers
         c->bin = 1 - c->bin;
         c->iin = 1 - c->iin;

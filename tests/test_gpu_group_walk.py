@@ -108,3 +108,37 @@ def test_group_theta_walk_matches_restatement(gbh_lib):
     e = np.linalg.norm(acc[body] - ref[body], axis=1) / np.linalg.norm(ref[body], axis=1)
     assert np.median(e) < 1e-5, np.median(e)
     assert np.percentile(e, 99.9) < 1e-3, np.percentile(e, 99.9)
+
+
+def test_group_walk_on_a_tree_built_for_the_plain_walk(gbh_lib):
+    # the start lists are built with the tree when a group walk is selected;
+    # a group walk on a tree built under the plain walk's parameters builds
+    # them itself, and a graph-launched plain step leaves them marked stale
+    n = 20000
+    bodies = ic.plummer(n, seed=8)
+    bounds = ic.exact_bounds(bodies)
+    p_plain = abi.step_params(theta=0.5, softening=1e-4, flags=abi.FLAG_STORE_ACCEL)
+    p_group = abi.step_params(theta=0.5, softening=1e-4, mac=abi.MAC_GROUP, flags=abi.FLAG_STORE_ACCEL)
+    a = BarnesHut(n, bounds, abi.units(G=1.0))
+    a.upload_bodies(bodies)
+    a.init()
+    for p in (p_group, p_plain, p_group, p_plain):  # graphs captured, then replayed
+        a.step(p)
+    a.synchronize()
+    state = a.read_bodies()
+    for x in (p_plain,):
+        a.stage_reset(x)
+        a.stage_prepare(x)
+    a.stage_sort()
+    a.stage_build()  # under the plain walk's parameters: no start lists
+    a.stage_fill()
+    a.stage_walk(p_group)
+    st = a.read_stats()
+    assert st.error_word == 0
+    acc = a.read_accel()[:, :3]
+    c = BarnesHut(n, bounds, abi.units(G=1.0))
+    c.upload_bodies(state)
+    c.init()
+    ref = c.evaluate_walk(p_group)
+    assert int(c.read_stats().interactions) == int(st.interactions)
+    assert np.array_equal(acc, ref)
