@@ -458,6 +458,164 @@ def kernels_per_step(mac_mode: int) -> int:
     return 1 + 3 + 9 + (1 if mac_mode == abi.MAC_PLAIN else 2) + 2 + 1 + 4
 
 
+def measure_e2e(bh, p_head, n, e2e_steps, local, dist=None) -> dict:
+    """The step end to end through the public API with host buffers: every
+    step's bodies go host->device from pinned memory and its result (all
+    bodies) comes back.  Headline form (streamed): each gbh_step_streamed
+    call runs one step while the next step's input goes up and the previous
+    step's result comes down on the copy engines; the first input is uploaded
+    before the first call and the last result read by
+    gbh_step_streamed_finish, both inside the timed region.  Also measured:
+    the exchange form (read-back and next upload overlapped with each other,
+    between steps) and the serial form.  Values per GPU."""
+    import torch
+
+    pin_in = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
+    pin_out = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
+    bh.read_bodies(out=pin_in)
+    bh.step(p_head)  # warm the graph of this parity
+    bh.read_bodies(out=pin_in)
+    # the first calls allocate the two extra body buffers and capture the
+    # step for each pairing of the rotating buffers (untimed)
+    for _ in range(6):
+        bh.step_streamed(p_head, pin_in, None)
+    bh.step_streamed_finish(None)
+    call_ms = []
+
+    def run(form):
+        # the harness's own garbage collector is paused for the timed calls
+        # (a collection of the process's heap is a host stall of tens of ms
+        # that a host in another language would not have)
+        gc.collect()
+        gc.disable()
+        try:
+            barrier(dist, local)
+            t0 = time.perf_counter()
+            if form == "streamed":
+                call_ms.append([])
+                bh.upload_bodies(pin_in, chunk=n)
+                for k in range(e2e_steps):
+                    tc = time.perf_counter()
+                    bh.step_streamed(p_head, pin_in if k + 1 < e2e_steps else None, pin_out if k else None)
+                    call_ms[-1].append(round((time.perf_counter() - tc) * 1e3, 2))
+                bh.step_streamed_finish(pin_out)
+            elif form == "exchange":
+                bh.upload_bodies(pin_in, chunk=n)
+                bh.step(p_head)
+                for _ in range(e2e_steps - 1):
+                    bh.exchange_bodies(pin_out, pin_in)
+                    bh.step(p_head)
+                bh.read_bodies(out=pin_out)
+            else:
+                for _ in range(e2e_steps):
+                    bh.upload_bodies(pin_in, chunk=n)
+                    bh.step(p_head)
+                    bh.read_bodies(out=pin_out)
+            return max_over_ranks(dist, time.perf_counter() - t0, local)
+        finally:
+            gc.enable()
+
+    serial_s = run("serial")
+    exchange_s = run("exchange")
+    # the headline form five times (a host stall in one run of 20 steps
+    # moves it by up to a fifth): the median, with all five kept
+    clocks = ClockSampler(local)
+    clocks.start()
+    runs = [run("streamed") for _ in range(5)]
+    clk = clocks.stop()
+    return {
+        "value": e2e_steps / sorted(runs)[2],
+        "runs": [e2e_steps / t for t in runs],
+        "call_ms": call_ms,  # host time of each streamed call, per run
+        "clocks": clk,
+        "unit": "steps/s",
+        "h2d_bytes_per_step": n * abi.BODY_DTYPE.itemsize + C.sizeof(abi.StepParams),
+        "d2h_bytes_per_step": n * abi.BODY_DTYPE.itemsize,
+        "steps": e2e_steps,
+        "path": "BarnesHut.upload_bodies, then per step step_streamed (C-ABI gbh_step_streamed: the step, the next "
+                "input's upload and the previous result's read-back overlapped), then step_streamed_finish; "
+                "pinned host buffers, every step's whole state up and its whole result down; median of five "
+                "timed runs (runs)",
+        "exchange_value": e2e_steps / exchange_s,
+        "exchange_path": "per step gbh_exchange_bodies (read-back and next upload overlapped with each other) + "
+                         "gbh_step",
+        "serial_value": e2e_steps / serial_s,
+        "serial_path": "per step upload_bodies + step + read_bodies, one copy direction at a time",
+    }
+
+
+def e2e_in_child(bh, p_head, n, bounds, units, e2e_steps, local):
+    """measure_e2e in a child process that opens a context of the current
+    state (bodies, parameters, the learned criterion's weights and band) and
+    nothing else.  In the bench process itself the streamed calls met host
+    stalls of 14 to 110 ms, about one per second, after the calibration
+    (contexts destroyed, multi-GB host arrays freed); a process with one
+    context showed none.  Returns None when the child fails."""
+    import subprocess
+    import tempfile
+
+    d = tempfile.mkdtemp(prefix="gbh_e2e_")
+    try:
+        np.save(os.path.join(d, "state.npy"), bh.read_bodies())
+        np.save(os.path.join(d, "bounds.npy"), np.asarray(bounds, np.float32))
+        with open(os.path.join(d, "params.bin"), "wb") as f:
+            f.write(bytes(p_head))
+        with open(os.path.join(d, "units.bin"), "wb") as f:
+            f.write(bytes(units))
+        learned = p_head.mac_mode == abi.MAC_LEARNED
+        if learned:
+            np.save(os.path.join(d, "weights.npy"), bh.mac_get_weights())
+        cfg = {"n": n, "steps": e2e_steps, "device": local, "learned": learned,
+               "band": list(bh.mac_get_band()) if learned else None}
+        with open(os.path.join(d, "cfg.json"), "w") as f:
+            json.dump(cfg, f)
+        env = {k: v for k, v in os.environ.items()
+               if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "LOCAL_WORLD_SIZE", "GROUP_RANK", "ROLE_RANK")}
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--e2e-child", d], capture_output=True,
+                           text=True, env=env, timeout=1200)
+        if r.returncode != 0:
+            print(f"e2e child failed ({r.returncode}): {r.stderr[-2000:]}", file=sys.stderr)
+            return None
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+        out["process"] = "a child process with one context of the timed state"
+        return out
+    except (OSError, ValueError, subprocess.SubprocessError) as e:
+        print(f"e2e child failed: {e}", file=sys.stderr)
+        return None
+    finally:
+        for f in os.listdir(d):
+            os.remove(os.path.join(d, f))
+        os.rmdir(d)
+
+
+def e2e_child(d: str) -> int:
+    """The child of e2e_in_child: one context of the saved state, then
+    measure_e2e; prints its result as one JSON line."""
+    import torch
+
+    from gravity_gb300 import BarnesHut
+
+    with open(os.path.join(d, "cfg.json")) as f:
+        cfg = json.load(f)
+    local = int(cfg["device"])
+    torch.cuda.set_device(local)
+    state = np.load(os.path.join(d, "state.npy"))
+    bounds = np.load(os.path.join(d, "bounds.npy"))
+    with open(os.path.join(d, "params.bin"), "rb") as f:
+        p = abi.StepParams.from_buffer_copy(f.read())
+    with open(os.path.join(d, "units.bin"), "rb") as f:
+        units = type(abi.units(G=1.0)).from_buffer_copy(f.read())
+    bh = BarnesHut(int(cfg["n"]), bounds, units, device=local)
+    bh.upload_bodies(state)
+    bh.init()
+    if cfg["learned"]:
+        bh.mac_set_weights(np.load(os.path.join(d, "weights.npy")))
+        bh.mac_set_band(*cfg["band"])
+    print(json.dumps(measure_e2e(bh, p, int(cfg["n"]), int(cfg["steps"]), local)), flush=True)
+    bh.close()
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -624,93 +782,18 @@ def run_ours(args):
     if mac_name == "learned" and WALK_LEARNED_DRAM_BYTES_PER_BODY:
         traffic = WALK_LEARNED_DRAM_BYTES_PER_BODY * n_live
 
-    # ---- e2e through the public API with host buffers: every step's bodies go
-    # host->device from pinned memory and its result (all bodies) comes back.
-    # Headline form (streamed): each gbh_step_streamed call runs one step while
-    # the next step's input goes up and the previous step's result comes down
-    # on the copy engines; the first input is uploaded before the first call
-    # and the last result read by gbh_step_streamed_finish, both inside the
-    # timed region.  Also measured: the exchange form (read-back and next
-    # upload overlapped with each other, between steps) and the serial form.
+    # ---- e2e through the public API with host buffers (measure_e2e), in a
+    # child process that holds only a context of this state and its buffers
     n = wl["n"]
-    pin_in = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
-    pin_out = torch.empty(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.BODY_DTYPE)
-    bh.read_bodies(out=pin_in)
     e2e_steps = max(3, min(args.steps, 20))
-    bh.step(p_head)  # warm the graph of this parity
-    bh.read_bodies(out=pin_in)
-    # the first calls allocate the third body buffer and capture the step for
-    # each pairing of the rotating buffers (untimed)
-    for _ in range(6):
-        bh.step_streamed(p_head, pin_in, None)
-    bh.step_streamed_finish(None)
-
-    def e2e_run(form):
-        # the harness's own garbage collector is paused for the timed calls
-        # (a collection of this process's heap is a host stall of tens of ms
-        # that a host in another language would not have)
-        gc.collect()
-        gc.disable()
-        try:
-            return _e2e_run(form)
-        finally:
-            gc.enable()
-
-    call_ms = []
-
-    def _e2e_run(form):
-        barrier(dist, local)
-        t0 = time.perf_counter()
-        if form == "streamed":
-            call_ms.append([])
-            bh.upload_bodies(pin_in, chunk=n)
-            for k in range(e2e_steps):
-                tc = time.perf_counter()
-                bh.step_streamed(p_head, pin_in if k + 1 < e2e_steps else None, pin_out if k else None)
-                call_ms[-1].append(round((time.perf_counter() - tc) * 1e3, 2))
-            bh.step_streamed_finish(pin_out)
-        elif form == "exchange":
-            bh.upload_bodies(pin_in, chunk=n)
-            bh.step(p_head)
-            for _ in range(e2e_steps - 1):
-                bh.exchange_bodies(pin_out, pin_in)
-                bh.step(p_head)
-            bh.read_bodies(out=pin_out)
-        else:
-            for _ in range(e2e_steps):
-                bh.upload_bodies(pin_in, chunk=n)
-                bh.step(p_head)
-                bh.read_bodies(out=pin_out)
-        return max_over_ranks(dist, time.perf_counter() - t0, local)
-
-    e2e_serial_s = e2e_run("serial")
-    e2e_exchange_s = e2e_run("exchange")
-    # the headline form five times (a host stall in one run of 20 steps
-    # moves it by up to a tenth): the median, with all five kept
-    e2e_clocks = ClockSampler(local)
-    e2e_clocks.start()
-    e2e_runs = [e2e_run("streamed") for _ in range(5)]
-    e2e_clk = e2e_clocks.stop()
-    e2e_s = sorted(e2e_runs)[2]
-    e2e = {
-        "value": world * e2e_steps / e2e_s,
-        "runs": [world * e2e_steps / t for t in e2e_runs],
-        "call_ms": call_ms,  # host time of each streamed call, per run
-        "clocks": e2e_clk,
-        "unit": "steps/s",
-        "h2d_bytes_per_step": n * abi.BODY_DTYPE.itemsize + C.sizeof(abi.StepParams),
-        "d2h_bytes_per_step": n * abi.BODY_DTYPE.itemsize,
-        "steps": e2e_steps,
-        "path": "BarnesHut.upload_bodies, then per step step_streamed (C-ABI gbh_step_streamed: the step, the next "
-                "input's upload and the previous result's read-back overlapped), then step_streamed_finish; "
-                "pinned host buffers, every step's whole state up and its whole result down; median of five "
-                "timed runs (runs)",
-        "exchange_value": world * e2e_steps / e2e_exchange_s,
-        "exchange_path": "per step gbh_exchange_bodies (read-back and next upload overlapped with each other) + "
-                         "gbh_step",
-        "serial_value": world * e2e_steps / e2e_serial_s,
-        "serial_path": "per step upload_bodies + step + read_bodies, one copy direction at a time",
-    }
+    e2e = e2e_in_child(bh, p_head, n, bounds, units, e2e_steps, local)
+    if e2e is None:  # the child failed: measure here
+        e2e = measure_e2e(bh, p_head, n, e2e_steps, local, dist)
+        e2e["process"] = "the bench process (the child process failed)"
+    # whole job: N times the slowest rank's rate
+    for k in ("value", "exchange_value", "serial_value"):
+        e2e[k] = world / max_over_ranks(dist, 1.0 / e2e[k], local)
+    e2e["runs"] = [world * v for v in e2e["runs"]]
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, bodies, bounds, units, budget_s=args.cpu_budget)
@@ -828,7 +911,10 @@ def main():
                     help="record the training pairs on the timed state itself (default: other workloads)")
     ap.add_argument("--save-mac-weights", default=None, help="save the trained MLP weights (.npy)")
     ap.add_argument("--mac-epochs", type=int, default=12)
+    ap.add_argument("--e2e-child", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.e2e_child:
+        return e2e_child(args.e2e_child)
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
