@@ -81,7 +81,9 @@ struct GroupSmem {
     alignas(16) uint32_t frag[MAC_SMEM_FRAG_WORDS];
     __nv_bfloat16 x[GW_WARPS * 32 * 16];  // feature tile of the batch being decided
 };
+#ifndef GW_STACK_LEARNED
 #define GW_STACK_LEARNED 640
+#endif
 template <int MODE>
 struct GroupCfg {
     static constexpr int stack = MODE == GM_LEARNED ? GW_STACK_LEARNED : GW_STACK;
