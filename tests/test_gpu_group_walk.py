@@ -76,10 +76,12 @@ def _group_walk(internal, leaves, N, first, count, theta, soft):
     return listed
 
 
-def test_group_theta_walk_matches_restatement(gbh_lib):
-    n = 12001
+@pytest.mark.parametrize("n,theta", [(50, 0.6), (97, 0.6), (1001, 0.3), (12001, 0.6)])
+def test_group_theta_walk_matches_restatement(gbh_lib, n, theta):
+    # 50 bodies: the whole tree is one group; 97: the root's children are
+    # groups; larger trees have groups at many depths
     bodies = ic.plummer(n, seed=7)
-    theta, soft = 0.6, 1e-4
+    soft = 1e-4
     sim = BarnesHut(n, ic.exact_bounds(bodies), abi.units(G=1.0))
     sim.upload_bodies(bodies)
     sim.init()
